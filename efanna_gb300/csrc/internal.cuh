@@ -1,0 +1,128 @@
+// Internal declarations shared by the efanna_gb300 translation units.
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+namespace efg {
+
+// A device buffer that grows on demand (never shrinks until freed).
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  int reserve(size_t n) {
+    if (n <= cap) return EFG_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 8 + 64;
+    cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(EFG_ERR_NOMEM, "cudaMalloc of " + std::to_string(want * sizeof(T)) + " bytes failed");
+    }
+    cap = want;
+    return EFG_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Host-side tree node (load/save and the merge-level check).
+struct HNode {
+  int32_t div_dim;
+  float div_val;
+  uint64_t start, end;
+  int32_t left, right;  // global node indices, -1 for leaves
+  int32_t level;
+};
+
+// Trees held by an index.  Nodes of all trees share one index space; leaf lists are tree-major
+// (tree t's list is leaves[t*n .. t*n+n)).
+struct Forest {
+  uint32_t ntrees = 0;
+  uint64_t n = 0;
+  std::vector<int32_t> roots;           // per tree, global node index
+  std::vector<uint32_t> tree_of_root;   // unused placeholder for symmetry
+  DevBuf<DNode> nodes;                  // search layout
+  uint64_t nnodes = 0;
+  DevBuf<int32_t> d_roots;
+  DevBuf<uint32_t> leaves;              // ntrees * n
+  // SoA build-side arrays (kept after a device build; used by the leaf merge)
+  DevBuf<int32_t> n_left, n_right, n_level, n_tree;
+  DevBuf<uint32_t> n_start, n_end;
+  bool has_soa = false;
+  void release() {
+    nodes.release(); d_roots.release(); leaves.release();
+    n_left.release(); n_right.release(); n_level.release(); n_tree.release(); n_start.release(); n_end.release();
+    ntrees = 0; nnodes = 0; roots.clear(); has_soa = false;
+  }
+};
+
+struct Graph {
+  uint64_t n = 0, nnz = 0;
+  uint32_t fixed_k = 0;  // 0 when rows have different lengths
+  DevBuf<uint64_t> ptr;  // n + 1
+  DevBuf<uint32_t> ids;  // nnz
+  bool valid = false;
+  void release() { ptr.release(); ids.release(); valid = false; n = nnz = 0; fixed_k = 0; }
+};
+
+struct SearchParams {
+  int epochs = 4, init_num = 100, extend_to = 10, search_trees = 0, search_lv = -1, method = 0;
+};
+
+}  // namespace efg
+
+struct efg_index {
+  uint64_t n = 0;
+  uint32_t dim = 0, ld = 0;  // ld: padded row stride in floats (multiple of 4)
+  float* d_base = nullptr;
+  efg_build_params bp{};
+  efg::Forest forest;
+  efg::Graph graph;
+  efg::SearchParams sp;
+  cudaStream_t stream = nullptr;
+  std::vector<int32_t> last_results;
+  uint32_t last_k = 0;
+  uint64_t last_nq = 0;
+  efg_build_stats bstats{};
+  efg_search_stats sstats{};
+  // search scratch
+  efg::DevBuf<float> q_buf;
+  efg::DevBuf<int32_t> out_buf;
+  efg::DevBuf<unsigned long long> eval_counter;
+};
+
+namespace efg {
+
+// distance.cu
+int launch_l2_pairs(const float* base, uint32_t dim, uint32_t ld, const uint32_t* a, const uint32_t* b, uint64_t m,
+                    float* out, cudaStream_t s);
+int brute_force_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                    uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                    cudaStream_t s);
+
+// trees.cu: builds `ntrees` canonical trees over the index's base (fills idx->forest).
+int build_forest(efg_index* idx, uint32_t ntrees);
+// Uploads a host forest (after loadTrees) into the device search layout.
+int upload_forest(efg_index* idx, const std::vector<HNode>& nodes, const std::vector<int32_t>& roots,
+                  const std::vector<uint32_t>& leaves, uint32_t ntrees);
+// Copies the device forest into host nodes (global indices) + leaves.
+int download_forest(efg_index* idx, std::vector<HNode>& nodes, std::vector<uint32_t>& leaves);
+
+// search.cu
+int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
+                  cudaStream_t s, bool count_evals);
+
+// nndescent.cu
+struct NNDState;
+int build_graph_device(efg_index* idx);
+int nnd_init_host(efg_index* idx, efg_nnd_host_state* st);
+int nnd_iterate_host(efg_index* idx, efg_nnd_host_state* st, uint32_t iter, uint64_t* pairs);
+
+}  // namespace efg

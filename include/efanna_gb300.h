@@ -1,0 +1,169 @@
+/*
+ * efanna_gb300 — C ABI of the GB300 (sm_103a) kNN-graph build and graph search.
+ *
+ * Plain pointers, sizes and status codes only; no CUDA or C++ types cross this boundary
+ * (streams are passed as void*, device buffers as plain pointers).  Each entry point names the
+ * reference interface it replaces (paths inside the ZJULearning/efanna project).
+ *
+ * Conventions
+ *   - Every function that can fail returns an int status (EFG_OK on success) and leaves a
+ *     description in efg_last_error() (thread-local).
+ *   - Host buffers are never retained: index creation copies the base vectors to the device.
+ *   - "row_stride" arguments are in elements (floats), not bytes; stride >= dim.
+ *   - Ids are uint32 (graph rows) or int32 (search results), as in the reference's files.
+ *   - An index is single-caller: do not call into one index from two threads at once
+ *     (as FIndex, efanna.hpp:9-75).
+ */
+#ifndef EFANNA_GB300_H
+#define EFANNA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference reports these conditions by exit()/stdout
+ * (kdtreeub_index.hpp:108-111,141,179,202,367-369,703,772,815); here each is a return value. */
+#define EFG_OK 0
+#define EFG_ERR_ARG 1          /* invalid argument (sizes, k > pool, zero trees, ...)          */
+#define EFG_ERR_CUDA 2         /* a CUDA call failed; see efg_last_error()                      */
+#define EFG_ERR_MERGE_LEVEL 3  /* merge level deeper than a tree leaf (kdtreeub_index.hpp:108) */
+#define EFG_ERR_OPEN 4         /* file cannot be opened (exit -10086/-10087)                   */
+#define EFG_ERR_FORMAT 5       /* malformed trees/graph/index file (exit -11, -6, -1)           */
+#define EFG_ERR_STATE 6        /* operation needs trees/graph that the index does not hold      */
+#define EFG_ERR_TREE_COUNT 7   /* more search trees requested than built ("wrong tree number")  */
+#define EFG_ERR_NOMEM 8        /* device allocation failed                                      */
+#define EFG_ERR_DEVICE_LIMIT 9 /* a device-side iteration limit was hit (work queue, probing)   */
+
+/* Build parameters: KDTreeUbIndexParams (kdtreeub_index.hpp:14-35) + IndexParams
+ * (general/params.hpp:19-33).  Field meaning follows the reference:
+ *   K            graph degree exported to gs/saveGraph                      (IndexParams::K)
+ *   S            sample size per iteration; also the BFS leaf threshold     (IndexParams::S)
+ *   L            neighbour pool capacity                                    (IndexParams::L)
+ *   check_k      rank below which an insert marks its source as "found"     (IndexParams::Check_K)
+ *   epochs       NN-descent iterations                                      (build_epoches)
+ *   trees        trees built (and kept for search)                          ("trees")
+ *   trees_build  trees used for the leaf-merge initial graph, 0 = trees    ("treesb")
+ *   merge_level  conquer-to depth of the leaf merge                         ("ml")
+ *   leaf_size    DFS leaf size                                              (IndexParams::TNS)
+ *   reverse_cap  reverse-list cap in update()                               (base_index.hpp:442)
+ *   seed         seed of the counter-hash random streams                    (reference: 1998)  */
+typedef struct efg_build_params {
+  uint32_t K, S, L, check_k, epochs, trees, trees_build, merge_level, leaf_size, reverse_cap;
+  uint64_t seed;
+} efg_build_params;
+
+/* Per-phase build statistics (the reference prints CPU clock() per phase under -DINFO,
+ * kdtreeub_index.hpp:93-106, base_index.hpp:441-447; these are device times). */
+typedef struct efg_build_stats {
+  double trees_ms, init_ms, refine_ms, total_ms;
+  uint64_t join_pairs;      /* pair distances evaluated by the join (the reference's `cc`)     */
+  uint64_t join_records;    /* neighbour-list insert candidates kept after the radius filter    */
+  uint64_t merge_distances; /* leaf-merge distances of the initial graph                        */
+  int32_t max_merge_depth;  /* on EFG_ERR_MERGE_LEVEL: deepest usable merge level               */
+} efg_build_stats;
+
+/* Per-call search statistics. */
+typedef struct efg_search_stats {
+  double device_ms;         /* kernel time of the last search call                             */
+  uint64_t distance_evals;  /* query-to-base distances computed by the last search call         */
+  uint64_t queries;
+} efg_search_stats;
+
+typedef struct efg_index efg_index;
+
+/* Defaults of KDTreeUbIndexParams(true, 4) with IndexParams' member defaults. */
+void efg_default_build_params(efg_build_params* p);
+
+/* FIndex<float>(Matrix, Distance*, IndexParams) — efanna.hpp:14-20, matrix.hpp:21-39.
+ * Copies n rows of dim floats (row_stride floats apart) from host memory to the device. */
+int efg_index_create(const float* data, uint64_t n, uint32_t dim, uint64_t row_stride,
+                     const efg_build_params* params, efg_index** out);
+/* Same, from a device buffer (copied device-to-device into the index's padded layout). */
+int efg_index_create_device(const float* d_data, uint64_t n, uint32_t dim, uint64_t row_stride,
+                            const efg_build_params* params, efg_index** out);
+void efg_index_destroy(efg_index* idx);
+
+/* FIndex::buildTrees — efanna.hpp:28-31, kdtreeub_index.hpp:1192-1276. */
+int efg_build_trees(efg_index* idx);
+/* FIndex::buildIndex — efanna.hpp:24-27, kdtreeub_index.hpp:92-113 (initGraph + refineGraph). */
+int efg_build_graph(efg_index* idx);
+int efg_get_build_stats(const efg_index* idx, efg_build_stats* out);
+
+/* FIndex::setSearchParams — efanna.hpp:56-58, base_index.hpp:153-161 (extend_to is clamped to
+ * init_num).  search_method 0 = nnexp (kdtreeub_index.hpp:363-494), 1 = kgraph (:496-654). */
+int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_to, int search_trees,
+                          int search_lv, int search_method);
+
+/* FIndex::knnSearch — efanna.hpp:32-34, base_index.hpp:311-313.  Host queries in, host ids out
+ * (nq*k int32).  The ids are also kept for efg_save_results. */
+int efg_knn_search(efg_index* idx, const float* queries, uint64_t nq, uint32_t dim, uint64_t row_stride,
+                   uint32_t k, int32_t* out_ids);
+/* Device-resident variant: queries and out_ids are device pointers; runs on `stream`
+ * (a cudaStream_t, or NULL for the legacy default stream) and does not synchronise. */
+int efg_knn_search_device(efg_index* idx, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                          uint32_t k, int32_t* d_out_ids, void* stream);
+int efg_get_search_stats(const efg_index* idx, efg_search_stats* out);
+
+/* File I/O, byte-compatible with the reference's formats. */
+int efg_save_graph(efg_index* idx, const char* path);   /* saveGraph  kdtreeub_index.hpp:295-312 */
+int efg_load_graph(efg_index* idx, const char* path);   /* loadGraph  kdtreeub_index.hpp:243-277 */
+int efg_save_trees(efg_index* idx, const char* path);   /* saveTrees  kdtreeub_index.hpp:197-242 */
+int efg_load_trees(efg_index* idx, const char* path);   /* loadTrees  kdtreeub_index.hpp:139-196 */
+int efg_save_index(efg_index* idx, const char* path);   /* saveIndex  kdtreeub_index.hpp:771-825 */
+int efg_load_index(efg_index* idx, const char* path);   /* loadIndex  kdtreeub_index.hpp:701-770 */
+int efg_save_results(efg_index* idx, const char* path); /* saveResults base_index.hpp:136-151    */
+
+/* getGraphSize / getGraphRow — efanna.hpp:59-64, base_index.hpp:494-501. */
+uint64_t efg_graph_size(const efg_index* idx);
+/* Copies row `row` into out (up to cap ids); returns the row length, or -1 on error. */
+int64_t efg_graph_row(const efg_index* idx, uint64_t row, uint32_t* out, uint64_t cap);
+/* Whole graph as CSR: row_ptr[n+1] and ids[nnz] (host buffers; pass NULL to query nnz). */
+int efg_graph_csr(const efg_index* idx, uint64_t* row_ptr, uint32_t* ids, uint64_t* nnz);
+/* Trees held by the index (0 if none). */
+uint32_t efg_tree_count(const efg_index* idx);
+
+const char* efg_last_error(void);
+const char* efg_version(void);
+
+/* ---------------------------------------------------------------------------------------
+ * Kernel-level entry points (device pointers).  These expose the hot-path kernels on their
+ * own for integration and parity testing.
+ * --------------------------------------------------------------------------------------- */
+
+/* Squared L2 of m row pairs: out[i] = ||base[a[i]] - base[b[i]]||^2.
+ * L2DistanceAVX::compare / L2Distance::compare — general/distance.hpp:125-147, 299-323. */
+int efg_l2_pairs(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const uint32_t* d_a,
+                 const uint32_t* d_b, uint64_t m, float* d_out, void* stream);
+
+/* Exact k-NN by brute force (Matrix::brute_force_search, general/matrix.hpp:57-68), ordered by
+ * (dist, id).  If exclude_self is nonzero, query i is base row (first_row + i) and is skipped.
+ * Distances are FP32; candidates within the FP32 error band of the k-th are re-ranked in FP64. */
+int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
+                        uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
+                        int32_t* d_ids, float* d_dists, void* stream);
+
+/* NN-descent state on the host, for state-level parity checks (one layout with the oracle):
+ * pool arrays are n*(L+1), list arrays n*cap.  efg_nnd_init runs the leaf-merge initial
+ * graph on the index's trees (initGraph, kdtreeub_index.hpp:1367-1424); efg_nnd_iterate runs
+ * one join + update (base_index.hpp:328-437) in place. */
+typedef struct efg_nnd_host_state {
+  uint64_t n;
+  uint32_t L, cap;
+  float* pool_dist;
+  uint32_t* pool_id;
+  uint8_t* pool_flag;
+  uint32_t *Lcur, *Range;
+  float *radius, *radiusM;
+  uint8_t* found;
+  uint32_t *new_ids, *new_cnt, *old_ids, *old_cnt;
+} efg_nnd_host_state;
+int efg_nnd_init(efg_index* idx, efg_nnd_host_state* st);
+int efg_nnd_iterate(efg_index* idx, efg_nnd_host_state* st, uint32_t iter, uint64_t* pairs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EFANNA_GB300_H */

@@ -1,0 +1,281 @@
+"""efanna_gb300 — GB300 (sm_103a) kNN-graph build and graph search behind EFANNA's index API.
+
+Python mirror of the reference's ``FIndex<float>`` (efanna.hpp:9-75) over the C ABI declared in
+include/efanna_gb300.h.  The compute runs in libefanna_gb300.so (hand-written CUDA kernels);
+there is no CPU path: importing works without a GPU, but every compute call needs the library
+and a CUDA device and raises ``EfannaError`` otherwise.
+
+    idx = Index(data, IndexParams(trees=8, merge_level=8, epochs=8, check=25, L=30, K=10, S=10))
+    idx.build_index()                      # buildIndex(): trees + leaf merge + NN-descent
+    idx.set_search_params(epochs=4, init_num=1200, extend_to=200, search_trees=8)
+    ids = idx.knn_search(10, queries)      # knnSearch()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libefanna_gb300.so")
+
+EFG_OK, EFG_ERR_ARG, EFG_ERR_CUDA, EFG_ERR_MERGE_LEVEL, EFG_ERR_OPEN, EFG_ERR_FORMAT = 0, 1, 2, 3, 4, 5
+EFG_ERR_STATE, EFG_ERR_TREE_COUNT, EFG_ERR_NOMEM, EFG_ERR_DEVICE_LIMIT = 6, 7, 8, 9
+
+
+class EfannaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("efanna_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+class BuildParams(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("K", "S", "L", "check_k", "epochs", "trees", "trees_build",
+                                          "merge_level", "leaf_size", "reverse_cap")] + [("seed", C.c_uint64)]
+
+
+class BuildStats(C.Structure):
+    _fields_ = [("trees_ms", C.c_double), ("init_ms", C.c_double), ("refine_ms", C.c_double),
+                ("total_ms", C.c_double), ("join_pairs", C.c_uint64), ("join_records", C.c_uint64),
+                ("merge_distances", C.c_uint64), ("max_merge_depth", C.c_int32)]
+
+
+class SearchStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("distance_evals", C.c_uint64), ("queries", C.c_uint64)]
+
+
+class HostState(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("L", C.c_uint32), ("cap", C.c_uint32),
+                ("pool_dist", C.POINTER(C.c_float)), ("pool_id", C.POINTER(C.c_uint32)),
+                ("pool_flag", C.POINTER(C.c_uint8)), ("Lcur", C.POINTER(C.c_uint32)),
+                ("Range", C.POINTER(C.c_uint32)), ("radius", C.POINTER(C.c_float)),
+                ("radiusM", C.POINTER(C.c_float)), ("found", C.POINTER(C.c_uint8)),
+                ("new_ids", C.POINTER(C.c_uint32)), ("new_cnt", C.POINTER(C.c_uint32)),
+                ("old_ids", C.POINTER(C.c_uint32)), ("old_cnt", C.POINTER(C.c_uint32))]
+
+
+@dataclass
+class IndexParams:
+    """KDTreeUbIndexParams(rnn_used, trees, merge_level, epoches, check, L, K, trees_build, S)
+    (kdtreeub_index.hpp:14-35), with IndexParams' TNS and the update's reverse-list cap."""
+    trees: int = 4
+    merge_level: int = 4
+    epochs: int = 4
+    check: int = 25
+    L: int = 30
+    K: int = 10
+    trees_build: int = 0
+    S: int = 10
+    leaf_size: int = 10
+    reverse_cap: int = 100
+    seed: int = 1998
+
+    def to_c(self) -> BuildParams:
+        return BuildParams(self.K, self.S, self.L, self.check, self.epochs, self.trees,
+                           self.trees_build or self.trees, self.merge_level, self.leaf_size, self.reverse_cap,
+                           self.seed)
+
+
+_lib = None
+
+
+def lib():
+    """Loads libefanna_gb300.so (building it first if it is missing and nvcc is available)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIB_PATH)
+    vp, u64, u32, i32, f32p = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int, C.POINTER(C.c_float)
+    sig = {
+        "efg_default_build_params": (None, [C.POINTER(BuildParams)]),
+        "efg_index_create": (i32, [f32p, u64, u32, u64, C.POINTER(BuildParams), C.POINTER(vp)]),
+        "efg_index_create_device": (i32, [vp, u64, u32, u64, C.POINTER(BuildParams), C.POINTER(vp)]),
+        "efg_index_destroy": (None, [vp]),
+        "efg_build_trees": (i32, [vp]),
+        "efg_build_graph": (i32, [vp]),
+        "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
+        "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
+        "efg_knn_search": (i32, [vp, f32p, u64, u32, u64, u32, C.POINTER(C.c_int32)]),
+        "efg_knn_search_device": (i32, [vp, vp, u64, u64, u32, vp, vp]),
+        "efg_get_search_stats": (i32, [vp, C.POINTER(SearchStats)]),
+        "efg_save_graph": (i32, [vp, C.c_char_p]), "efg_load_graph": (i32, [vp, C.c_char_p]),
+        "efg_save_trees": (i32, [vp, C.c_char_p]), "efg_load_trees": (i32, [vp, C.c_char_p]),
+        "efg_save_index": (i32, [vp, C.c_char_p]), "efg_load_index": (i32, [vp, C.c_char_p]),
+        "efg_save_results": (i32, [vp, C.c_char_p]),
+        "efg_graph_size": (u64, [vp]),
+        "efg_graph_row": (C.c_int64, [vp, u64, C.POINTER(C.c_uint32), u64]),
+        "efg_graph_csr": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]),
+        "efg_tree_count": (u32, [vp]),
+        "efg_last_error": (C.c_char_p, []),
+        "efg_version": (C.c_char_p, []),
+        "efg_l2_pairs": (i32, [vp, u64, u32, u64, vp, vp, u64, vp, vp]),
+        "efg_brute_force_knn": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_nnd_init": (i32, [vp, C.POINTER(HostState)]),
+        "efg_nnd_iterate": (i32, [vp, C.POINTER(HostState), u32, C.POINTER(C.c_uint64)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != EFG_OK:
+        raise EfannaError(rc, lib().efg_last_error().decode())
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Index:
+    """FIndex<float> over the GPU implementation (efanna.hpp:9-75)."""
+
+    def __init__(self, data: np.ndarray, params: IndexParams | None = None):
+        data = np.ascontiguousarray(data, dtype=np.float32)
+        if data.ndim != 2:
+            raise ValueError("data must be 2-D (rows x dim)")
+        self.n, self.dim = data.shape
+        self.params = params or IndexParams()
+        self._h = C.c_void_p()
+        p = self.params.to_c()
+        _check(lib().efg_index_create(_fp(data), self.n, self.dim, self.dim, C.byref(p), C.byref(self._h)))
+
+    @classmethod
+    def from_device(cls, ptr: int, n: int, dim: int, row_stride: int, params: IndexParams | None = None):
+        self = cls.__new__(cls)
+        self.n, self.dim = n, dim
+        self.params = params or IndexParams()
+        self._h = C.c_void_p()
+        p = self.params.to_c()
+        _check(lib().efg_index_create_device(C.c_void_p(ptr), n, dim, row_stride, C.byref(p), C.byref(self._h)))
+        return self
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().efg_index_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # buildIndex / buildTrees
+    def build_index(self) -> None:
+        _check(lib().efg_build_graph(self._h))
+
+    def build_trees(self) -> None:
+        _check(lib().efg_build_trees(self._h))
+
+    def build_stats(self) -> BuildStats:
+        s = BuildStats()
+        _check(lib().efg_get_build_stats(self._h, C.byref(s)))
+        return s
+
+    def search_stats(self) -> SearchStats:
+        s = SearchStats()
+        _check(lib().efg_get_search_stats(self._h, C.byref(s)))
+        return s
+
+    def set_search_params(self, epochs: int, init_num: int, extend_to: int, search_trees: int = 0,
+                          search_lv: int = -1, search_method: int = 0) -> None:
+        _check(lib().efg_set_search_params(self._h, epochs, init_num, extend_to, search_trees, search_lv,
+                                           search_method))
+
+    def knn_search(self, k: int, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        out = np.zeros((q.shape[0], k), dtype=np.int32)
+        _check(lib().efg_knn_search(self._h, _fp(q), q.shape[0], q.shape[1], q.shape[1], k,
+                                    out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def knn_search_device(self, k: int, q_ptr: int, nq: int, row_stride: int, out_ptr: int, stream: int = 0):
+        _check(lib().efg_knn_search_device(self._h, C.c_void_p(q_ptr), nq, row_stride, k, C.c_void_p(out_ptr),
+                                           C.c_void_p(stream)))
+
+    # files
+    def save_graph(self, path: str): _check(lib().efg_save_graph(self._h, path.encode()))
+    def load_graph(self, path: str): _check(lib().efg_load_graph(self._h, path.encode()))
+    def save_trees(self, path: str): _check(lib().efg_save_trees(self._h, path.encode()))
+    def load_trees(self, path: str): _check(lib().efg_load_trees(self._h, path.encode()))
+    def save_index(self, path: str): _check(lib().efg_save_index(self._h, path.encode()))
+    def load_index(self, path: str): _check(lib().efg_load_index(self._h, path.encode()))
+    def save_results(self, path: str): _check(lib().efg_save_results(self._h, path.encode()))
+
+    def graph_size(self) -> int:
+        return int(lib().efg_graph_size(self._h))
+
+    def graph_row(self, row: int) -> list:
+        n = lib().efg_graph_row(self._h, row, None, 0)
+        if n < 0:
+            _check(EFG_ERR_ARG)
+        buf = (C.c_uint32 * max(1, n))()
+        lib().efg_graph_row(self._h, row, buf, n)
+        return list(buf[:n])
+
+    def graph_csr(self):
+        nnz = C.c_uint64()
+        _check(lib().efg_graph_csr(self._h, None, None, C.byref(nnz)))
+        ptr = np.zeros(self.graph_size() + 1, np.uint64)
+        ids = np.zeros(max(1, nnz.value), np.uint32)
+        _check(lib().efg_graph_csr(self._h, ptr.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                   ids.ctypes.data_as(C.POINTER(C.c_uint32)), None))
+        return ptr, ids[:nnz.value]
+
+    def graph(self) -> np.ndarray:
+        """Fixed-degree graph as an (n, K) array."""
+        ptr, ids = self.graph_csr()
+        return ids.reshape(self.graph_size(), -1)
+
+    def tree_count(self) -> int:
+        return int(lib().efg_tree_count(self._h))
+
+    # state-level NN-descent (parity tests)
+    def nnd_init(self, st) -> None:
+        hs = _host_state(st)
+        _check(lib().efg_nnd_init(self._h, C.byref(hs)))
+
+    def nnd_iterate(self, st, it: int) -> int:
+        hs = _host_state(st)
+        pairs = C.c_uint64()
+        _check(lib().efg_nnd_iterate(self._h, C.byref(hs), it, C.byref(pairs)))
+        return int(pairs.value)
+
+
+def _host_state(st) -> HostState:
+    """Wraps an object with the state arrays (n, Lcap, cap, pool_dist, ...) of one layout."""
+    def p(a, t):
+        assert a.flags.c_contiguous
+        return a.ctypes.data_as(C.POINTER(t))
+    return HostState(st.n, st.Lcap, st.cap, p(st.pool_dist, C.c_float), p(st.pool_id, C.c_uint32),
+                     p(st.pool_flag, C.c_uint8), p(st.L, C.c_uint32), p(st.Range, C.c_uint32),
+                     p(st.radius, C.c_float), p(st.radiusM, C.c_float), p(st.found, C.c_uint8),
+                     p(st.new_ids, C.c_uint32), p(st.new_cnt, C.c_uint32), p(st.old_ids, C.c_uint32),
+                     p(st.old_cnt, C.c_uint32))
+
+
+def l2_pairs_device(base_ptr: int, n: int, dim: int, row_stride: int, a_ptr: int, b_ptr: int, m: int,
+                    out_ptr: int, stream: int = 0) -> None:
+    _check(lib().efg_l2_pairs(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(a_ptr), C.c_void_p(b_ptr), m,
+                              C.c_void_p(out_ptr), C.c_void_p(stream)))
+
+
+def brute_force_knn_device(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int, q_stride: int,
+                           k: int, ids_ptr: int, dists_ptr: int = 0, exclude_self: bool = False, first_row: int = 0,
+                           stream: int = 0) -> None:
+    _check(lib().efg_brute_force_knn(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(q_ptr), nq, q_stride, k,
+                                     int(exclude_self), first_row, C.c_void_p(ids_ptr),
+                                     C.c_void_p(dists_ptr or None), C.c_void_p(stream)))
+
+
+def version() -> str:
+    return lib().efg_version().decode()

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(BF_THREADS) bf_chunk_kernel(const float* __res
   uint64_t q0 = (uint64_t)blockIdx.x * BF_QB;
   uint64_t r0 = (uint64_t)blockIdx.y * chunk;
   uint64_t r1 = min(n, r0 + chunk);
-  uint32_t nqb = (uint32_t)min<uint64_t>(BF_QB, nq - q0);
+  uint32_t nqb = (uint32_t)((nq - q0) < (uint64_t)BF_QB ? (nq - q0) : (uint64_t)BF_QB);
   for (uint32_t i = threadIdx.x; i < BF_QB * ld4; i += blockDim.x) {
     uint32_t qq = i / ld4, c = i % ld4;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(BF_THREADS) bf_chunk_kernel(const float* __res
     uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t qq = warp; qq < BF_QB; qq += BF_THREADS / 32) {
       uint64_t* buf = cand + (size_t)qq * BF_CAP;
-      uint32_t c = min<uint32_t>(cnt[qq], BF_CAP);
+      uint32_t c = cnt[qq] < (uint32_t)BF_CAP ? cnt[qq] : (uint32_t)BF_CAP;
       uint32_t p2 = 1;
       while (p2 < c) p2 <<= 1;
       for (uint32_t i = c + lane; i < p2; i += 32) buf[i] = ~0ULL;

@@ -31,6 +31,7 @@ static int check_params(const efg_build_params* p, uint64_t n) {
   if (p->trees < 1 || p->trees > 1024) return fail(EFG_ERR_ARG, "trees must be in [1, 1024]");
   if (p->trees_build > p->trees) return fail(EFG_ERR_ARG, "trees_build must be <= trees");
   if (p->leaf_size < 1) return fail(EFG_ERR_ARG, "leaf_size must be >= 1");
+  if (p->reverse_cap < 1 || p->reverse_cap > 4096) return fail(EFG_ERR_ARG, "reverse_cap must be in [1, 4096]");
   if (n < 2 * (uint64_t)p->S + 2) return fail(EFG_ERR_ARG, "need at least 2*S+2 points");
   if (n >= (1ULL << 30)) return fail(EFG_ERR_ARG, "at most 2^30 - 1 points");
   return EFG_OK;

@@ -86,11 +86,17 @@ static float l2_scalar(const float* a, const float* b, size_t size) {
   return result;
 }
 
+// Sequential mode measures with L2DistanceAVX, the class every reference sample uses; canonical
+// mode with the plain squared L2 (L2Distance), which the CUDA kernels compute (in any summation
+// order the two agree exactly on integer-valued data).  They differ beyond rounding only for
+// d mod 32 in {9..24}, where L2DistanceAVX drops part of the tail.
 struct Data {
   const float* p;
   size_t n, d, ld;
+  int mode;
   const float* row(size_t i) const { return p + i * ld; }
-  float dist(size_t i, size_t j) const { return l2_avx(row(i), row(j), d); }
+  float distq(const float* a, const float* b) const { return mode == 0 ? l2_avx(a, b, d) : l2_scalar(a, b, d); }
+  float dist(size_t i, size_t j) const { return distq(row(i), row(j)); }
 };
 
 // ----------------------------------------------------------------------------------------------
@@ -666,7 +672,8 @@ static uint64_t join_canon(const Data& X, State& st, const Params& p) {
 // ---- update ----
 // InitIndex::update (base_index.hpp:373-437).  In sequential mode reverse lists are cut with
 // random_shuffle; in canonical mode they are sorted by source id and, when longer than the cap,
-// reduced to the `cap` sources with the smallest counter hash, ordered by (hash, source).
+// reduced to the `cap` sources with the smallest (high 32 bits of the counter hash, source),
+// in that order.
 static void update(State& st, const Params& p, int mode, uint32_t iter) {
   size_t n = st.n;
   std::vector<std::vector<uint32_t>> rnn_new(n), rnn_old(n);
@@ -714,7 +721,7 @@ static void update(State& st, const Params& p, int mode, uint32_t iter) {
       } else if (cap && R.size() > cap) {
         uint64_t tag = which == 0 ? TAG_RNEW : TAG_ROLD;
         std::vector<std::pair<uint64_t, uint32_t>> h;
-        for (uint32_t s : R) h.push_back({hash4(p.seed, tag, iter, i, s), s});
+        for (uint32_t s : R) h.push_back({hash4(p.seed, tag, iter, i, s) >> 32, s});
         std::sort(h.begin(), h.end());
         R.clear();
         for (unsigned k = 0; k < cap; ++k) R.push_back(h[k].second);
@@ -907,7 +914,8 @@ static int init_graph(const Data& X, const Forest& F, const Params& p, int mode,
     std::vector<uint32_t> extra;
     if (R.size() >= p.S + 2 * (size_t)p.S) {
       std::vector<std::pair<uint64_t, uint32_t>> h;
-      for (size_t k = p.S; k < R.size(); ++k) h.push_back({hash4(p.seed, TAG_EXTRA, nn, R[k].second, 0), R[k].second});
+      for (size_t k = p.S; k < R.size(); ++k)
+        h.push_back({hash4(p.seed, TAG_EXTRA, nn, R[k].second, 0) >> 32, R[k].second});
       std::sort(h.begin(), h.end());
       for (unsigned k = 0; k < p.S; ++k) extra.push_back(h[k].second);
     } else {
@@ -1016,7 +1024,7 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
   unsigned resultSize = (unsigned)a.extend_to;
   if (a.k > resultSize) resultSize = a.k;
   std::vector<std::pair<float, size_t>> result;
-  for (unsigned j = 0; j < pool.size(); ++j) result.push_back({l2_avx(q, X.row(pool[j]), X.d), (size_t)pool[j]});
+  for (unsigned j = 0; j < pool.size(); ++j) result.push_back({X.distq(q, X.row(pool[j])), (size_t)pool[j]});
   uint64_t evals = pool.size();
   std::partial_sort(result.begin(), result.begin() + resultSize, result.end());
   result.resize(resultSize);
@@ -1037,7 +1045,7 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
         }
       }
     }
-    for (size_t j = 0; j < ids.size(); ++j) result.push_back({l2_avx(q, X.row(ids[j]), X.d), (size_t)ids[j]});
+    for (size_t j = 0; j < ids.size(); ++j) result.push_back({X.distq(q, X.row(ids[j])), (size_t)ids[j]});
     evals += ids.size();
     std::partial_sort(result.begin(), result.begin() + resultSize, result.end());
     result.resize(resultSize);
@@ -1083,7 +1091,7 @@ void orc_l2_pairs(const float* base, uint64_t ld, uint64_t d, const uint32_t* ia
 
 void* orc_forest_build(const float* data, uint64_t n, uint32_t d, uint64_t ld, uint32_t trees, uint32_t S,
                        uint32_t tns, int mode, uint64_t seed) {
-  Data X{data, n, d, ld};
+  Data X{data, n, d, ld, mode};
   Forest* F = new Forest();
   if (mode == MODE_SEQ) {
     srand(1);
@@ -1103,7 +1111,7 @@ void orc_forest_free(void* f) { delete (Forest*)f; }
 // stats[0] = join pair distances over all iterations, stats[1] = merge-depth limit on error.
 int orc_build_graph(const float* data, uint64_t n, uint32_t d, uint64_t ld, const orc_params* pp, int mode,
                     uint32_t* gs_out, void** forest_out, uint64_t* stats) {
-  Data X{data, n, d, ld};
+  Data X{data, n, d, ld, mode};
   Params p = to_params(pp);
   Forest* F = new Forest();
   if (mode == MODE_SEQ) {
@@ -1166,7 +1174,7 @@ static int state_out(State& st, float* pd, uint32_t* pid, uint8_t* pf, uint32_t*
 int orc_nnd_init(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* forest, const orc_params* pp, int mode,
                  float* pd, uint32_t* pid, uint8_t* pf, uint32_t* L, uint32_t* R, float* rad, float* radM,
                  uint8_t* found, uint32_t* nid, uint32_t* ncnt, uint32_t* oid, uint32_t* ocnt, uint32_t cap) {
-  Data X{data, n, d, ld};
+  Data X{data, n, d, ld, mode};
   Params p = to_params(pp);
   State st;
   int rc = init_graph(X, *(Forest*)forest, p, mode, st, nullptr);
@@ -1179,7 +1187,7 @@ int orc_nnd_iterate(const float* data, uint64_t n, uint32_t d, uint64_t ld, cons
                     uint32_t iter, float* pd, uint32_t* pid, uint8_t* pf, uint32_t* L, uint32_t* R, float* rad,
                     float* radM, uint8_t* found, uint32_t* nid, uint32_t* ncnt, uint32_t* oid, uint32_t* ocnt,
                     uint32_t cap, uint64_t* pairs) {
-  Data X{data, n, d, ld};
+  Data X{data, n, d, ld, mode};
   Params p = to_params(pp);
   State st;
   state_in(st, n, p.L, pd, pid, pf, L, R, rad, radM, found, nid, ncnt, oid, ocnt, cap);
@@ -1197,7 +1205,7 @@ int orc_search(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* for
                const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, int epochs, int init_num,
                int extend_to, int search_trees, uint32_t k, int mode, int threads, uint64_t seed, int32_t* out,
                uint64_t* evals) {
-  Data X{data, n, d, ld};
+  Data X{data, n, d, ld, mode};
   Forest* F = (Forest*)forest;
   if (search_trees <= 0 || (size_t)search_trees > F->nodes.size()) return -1;
   if (extend_to > init_num) extend_to = init_num;  // setSearchParams (base_index.hpp:156-157)

@@ -1,0 +1,120 @@
+"""The CPU oracle against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference compiled here, single-threaded)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+from efanna_gb300 import io
+
+CASES = ["small_d32", "mid_d128"]
+
+
+def _params(O, gp):
+    trees, ml, ep, L, ck, K, S = [int(v) for v in gp]
+    return O.make_params(K=K, S=S, L=L, check_k=ck, epochs=ep, trees=trees, merge_level=ml)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_seq_graph_matches_reference_bytes(oracle_lib, case):
+    O = oracle_lib
+    g = load_golden(case)
+    x = g["base"].astype(np.float32)
+    rc, gs, forest, _ = O.build_graph(x, _params(O, g["graph_params"]), O.SEQ)
+    assert rc == 0
+    ref = np.fromfile(os.path.join(GOLDEN, case + ".graph"), np.uint32).reshape(x.shape[0], -1)
+    assert np.all(ref[:, 0] == gs.shape[1])
+    assert np.array_equal(ref[:, 1:], gs)
+
+
+def _tree_records(path):
+    """Trees file with the raw child-pointer words reduced to null / non-null."""
+    import struct
+    A = bytearray(open(path, "rb").read())
+    K, T, N, D = struct.unpack_from("<IIQQ", A, 0)
+    off = 24
+    for _ in range(T):
+        nn, _ns = struct.unpack_from("<ii", A, off)
+        off += 8
+        for _ in range(nn):
+            lp, rp = struct.unpack_from("<QQ", A, off + 24)
+            struct.pack_into("<QQ", A, off + 24, int(lp != 0), int(rp != 0))
+            off += 40
+    return bytes(A)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_seq_trees_match_reference_bytes(oracle_lib, case, tmp_path):
+    O = oracle_lib
+    g = load_golden(case)
+    x = g["base"].astype(np.float32)
+    rc, gs, forest, _ = O.build_graph(x, _params(O, g["graph_params"]), O.SEQ)
+    out = str(tmp_path / "o.trees")
+    forest.save(out, int(g["graph_params"][5]))
+    assert _tree_records(out) == _tree_records(os.path.join(GOLDEN, case + ".trees"))
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("mode", ["seq", "canon"])
+def test_search_matches_reference_results(oracle_lib, case, mode):
+    O = oracle_lib
+    g = load_golden(case)
+    x = g["base"].astype(np.float32)
+    q = g["queries"].astype(np.float32)
+    st, se, pool, ext, k = [int(v) for v in g["search_params"]]
+    forest = O.Forest.load(os.path.join(GOLDEN, case + ".trees"))
+    gp, gi = io.read_graph_csr(os.path.join(GOLDEN, case + ".graph"))
+    out = O.search(x, forest, gp, gi, q, k=k, epochs=se, init_num=pool, extend_to=ext, trees=st,
+                   mode=O.SEQ if mode == "seq" else O.CANON, threads=1 if mode == "seq" else 4)
+    assert np.array_equal(out, g["results"])
+
+
+def test_merge_level_error_matches_reference(oracle_lib):
+    """The reference aborts with 'merge level deeper than tree, max merge deepth is 5' on this case."""
+    O = oracle_lib
+    g = load_golden("small_d32")
+    x = g["base"].astype(np.float32)
+    rc, gs, forest, maxd = O.build_graph(x, O.make_params(merge_level=8), O.SEQ)
+    assert rc == 3 and maxd == 5
+    rc, gs, forest, maxd = O.build_graph(x, O.make_params(merge_level=8), O.CANON)
+    assert rc == 3
+
+
+def test_canonical_recall_equivalent(oracle_lib):
+    """The order-independent restatement reaches the same graph quality as the reference order."""
+    O = oracle_lib
+    from efanna_gb300 import datasets
+    x = datasets.mixture_u8(6000, 64, seed=3)
+    xd = x.astype(np.float64)
+    D = (xd * xd).sum(1)[:, None] + (xd * xd).sum(1)[None, :] - 2 * xd @ xd.T
+    np.fill_diagonal(D, np.inf)
+    gt = np.argpartition(D, 10, axis=1)[:, :10]
+    p = O.make_params(merge_level=5, epochs=6)
+    rec = {}
+    for mode in (O.SEQ, O.CANON):
+        rc, gs, _, _ = O.build_graph(x, p, mode)
+        assert rc == 0
+        rec[mode] = np.mean([len(set(gs[i]) & set(gt[i])) for i in range(len(x))]) / 10
+    assert abs(rec[O.SEQ] - rec[O.CANON]) < 0.01, rec
+
+
+def test_l2_orders_agree_on_integers(oracle_lib):
+    O = oracle_lib
+    rng = np.random.default_rng(0)
+    for d in (8, 32, 128, 96, 960):
+        a = rng.integers(0, 256, d).astype(np.float32)
+        b = rng.integers(0, 256, d).astype(np.float32)
+        exact = float(((a.astype(np.int64) - b.astype(np.int64)) ** 2).sum())
+        assert O.l2(a, b, "avx") == exact
+        assert O.l2(a, b, "scalar") == exact
+
+
+def test_l2_avx_tail_quirk(oracle_lib):
+    """L2DistanceAVX sums only 8 of the 16/24 padded tail floats (distance.hpp:305-314)."""
+    O = oracle_lib
+    d = 48  # D % 32 == 16
+    a = np.ones(d, np.float32)
+    b = np.zeros(d, np.float32)
+    assert O.l2(a, b, "scalar") == 48.0
+    assert O.l2(a, b, "avx") == 40.0

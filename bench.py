@@ -1,0 +1,370 @@
+"""Benchmark: kNN-graph build and batched graph search on one GB300 (EFANNA hot path).
+
+Workload (the reference's 1M x 128 configuration): N = 1,000,000 base vectors, d = 128, from the
+seeded integer-valued Gaussian mixture (efanna_gb300.datasets.mixture_u8, seed 0), K = 10 graph
+built with trees=8, merge level 8, 8 iterations, L=30, check=25, S=10; 16 search trees built
+separately; 10,000 held-out queries (seed 1); k = 10.  Recall is measured against the exact
+10-NN (GPU brute force, FP64 re-rank at the boundary).
+
+A step is one batched search of all queries at the operating point that reaches recall@10 >= 0.95
+(searched with 16 trees).  `value` is queries/s with queries and results resident on the device;
+`e2e` is the same through efg_knn_search with host buffers (host->device copy of the queries and
+device->host copy of the ids inside the timed region).  The graph build is timed separately and
+reported under "build".  The base set (512 MB) is larger than the 129 MB L2, so no L2 flush is
+needed between steps.
+
+--impl reference times the CPU baseline: the oracle's OpenMP restatement of the reference
+(ORC_OMP: the reference's parallel build and nnexp search), on all host cores, same workload and
+operating point, each step a bounded sample of the queries.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "graph build s & QPS at recall@10>=0.95, 1xGB300: plain FP32 vs BF16+learned"
+GRAPH = dict(trees=8, merge_level=8, epochs=8, check=25, L=30, K=10, S=10)
+SEARCH_TREES = 16
+CONFIG_POINT = (4, 1200, 200)  # the reference configuration's epochs / pool / extend
+LADDER = [(4, 1200, 200), (4, 2400, 400), (6, 4000, 400), (6, 4000, 600), (8, 6000, 600), (8, 8000, 800),
+          (8, 12000, 1200), (12, 16000, 1600)]
+TARGET = 0.95
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def recall(res: np.ndarray, gt: np.ndarray, k: int = 10) -> float:
+    hits = 0
+    for r, g in zip(res[:, :k], gt[:, :k]):
+        hits += len(set(r.tolist()) & set(g.tolist()))
+    return hits / (k * len(res))
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--id=0", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def make_data(n, nq):
+    from efanna_gb300 import datasets
+    x = datasets.mixture_u8(n, 128, seed=0)
+    q = datasets.mixture_u8(nq, 128, seed=0, queries=True)
+    return x, q
+
+
+# --------------------------------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    import efanna_gb300 as E
+
+    ws, rank = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda")
+    x, q = make_data(args.n, args.nq)
+    nq = q.shape[0]
+    X = torch.from_numpy(x).to(dev)
+
+    # graph build (timed separately), then the 16 search trees
+    idx = E.Index.from_device(X.data_ptr(), args.n, 128, 128, E.IndexParams(**GRAPH))
+    build_s = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        idx.build_index()
+        torch.cuda.synchronize()
+        build_s.append(time.perf_counter() - t0)
+    bst = idx.build_stats()
+    graph = idx.graph()
+    t0 = time.perf_counter()
+    idx.build_trees(SEARCH_TREES)
+    torch.cuda.synchronize()
+    trees_s = time.perf_counter() - t0
+
+    # exact ground truth on the GPU
+    Q = torch.from_numpy(q).to(dev)
+    gt = torch.zeros((nq, 10), dtype=torch.int32, device=dev)
+    E.brute_force_knn_device(X.data_ptr(), args.n, 128, 128, Q.data_ptr(), nq, 128, 10, gt.data_ptr())
+    samp = np.random.default_rng(0).choice(args.n, min(args.n, 10000), replace=False)
+    S = X[torch.from_numpy(samp).to(dev)].contiguous()
+    gt11 = torch.zeros((len(samp), 11), dtype=torch.int32, device=dev)
+    E.brute_force_knn_device(X.data_ptr(), args.n, 128, 128, S.data_ptr(), len(samp), 128, 11, gt11.data_ptr())
+    torch.cuda.synchronize()
+    gt = gt.cpu().numpy()
+    g11 = gt11.cpu().numpy()
+    graph_recall = float(np.mean([len(set(graph[s].tolist()) & set([v for v in g11[i] if v != s][:10]))
+                                  for i, s in enumerate(samp)]) / 10)
+
+    out = torch.zeros((nq, 10), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def search_once(point):
+        idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
+        idx.knn_search_device(10, Q.data_ptr(), nq, 128, out.data_ptr(), stream.cuda_stream)
+
+    # operating point: first ladder entry reaching the target recall
+    ladder = []
+    point = None
+    for pt in LADDER:
+        try:
+            search_once(pt)
+            torch.cuda.synchronize()
+        except E.EfannaError as e:
+            log("skip", pt, e)
+            continue
+        rc = recall(out.cpu().numpy(), gt)
+        ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4)})
+        if rc >= TARGET:
+            point = pt
+            break
+    if point is None:
+        point = LADDER[-1]
+    res_cfg = None
+    search_once(CONFIG_POINT)
+    torch.cuda.synchronize()
+    res_cfg = recall(out.cpu().numpy(), gt)
+    # evals / expansions at the operating point (host API fills the stats)
+    idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
+    res_host = idx.knn_search(10, q)
+    st = idx.search_stats()
+    op_recall = recall(res_host, gt)
+    evals_q = st.distance_evals / nq
+    exp_q = st.expanded_nodes / nq
+    # algorithmic bytes per query: candidate rows + graph rows of expanded nodes + leaf ids + query
+    bytes_q = evals_q * 128 * 4 + exp_q * GRAPH["K"] * 4 + point[1] * 4 + 128 * 4
+
+    # the timed region
+    for _ in range(args.warmup):
+        search_once(point)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler()
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        search_once(point)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ck = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_t = torch.tensor([ms], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    per_step_ms = ms / args.steps
+    value = ws * nq * args.steps / (ms / 1e3)
+    launch_ms = per_step_ms  # one nnexp launch per step, timed on its own stream
+
+    # end to end through the host API
+    for _ in range(max(1, args.warmup // 2)):
+        idx.knn_search(10, q)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        idx.knn_search(10, q)
+    e2e_s = time.perf_counter() - t0
+    e2e = ws * nq * args.steps / e2e_s
+
+    hbm, peak_kind = peaks()
+    achieved = bytes_q * nq / (launch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_step_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded integer-valued Gaussian mixture)",
+        "config": {"workload": "1M x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), "
+                               "16 search trees, 10k queries, k=10",
+                   "n": args.n, "dim": 128, "queries": nq, "k": 10, "search_trees": SEARCH_TREES,
+                   "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2],
+                                       "recall@10": round(op_recall, 4)},
+                   "config_point": {"epochs": CONFIG_POINT[0], "pool": CONFIG_POINT[1], "extend": CONFIG_POINT[2],
+                                    "recall@10": round(res_cfg, 4)},
+                   "ladder": ladder, "l2": "inputs larger than L2 (512 MB base), no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "build": {"graph_build_s": round(min(build_s), 4), "graph_build_s_runs": [round(b, 4) for b in build_s],
+                  "trees_ms": round(bst.trees_ms, 2), "init_ms": round(bst.init_ms, 2),
+                  "refine_ms": round(bst.refine_ms, 2), "join_pairs": int(bst.join_pairs),
+                  "graph_recall@10": round(graph_recall, 4), "search_trees16_s": round(trees_s, 4)},
+        "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                "d2h_bytes_per_step": int(nq * 10 * 4)},
+        "roofline": {"bound": "hbm", "kernel": "nnexp_kernel", "achieved": round(achieved, 1), "peak": hbm,
+                     "peak_kind": peak_kind + " (burst)", "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "algorithmic_bytes_per_query": round(bytes_q, 1), "distance_evals_per_query": round(evals_q, 1),
+                     "expanded_per_query": round(exp_q, 1),
+                     "traffic": None},
+        "gpu_launches": args.steps,
+        "clocks": ck,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x, q, gt, point, idx, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    idx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(x, q, gt, point, idx, args):
+    """The oracle's search (reference nnexp semantics, OpenMP over queries) on the GPU-built trees
+    and graph, over a bounded sample of the queries."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as tmp:
+        idx.save_trees(os.path.join(tmp, "t.trees"))
+        forest = O.Forest.load(os.path.join(tmp, "t.trees"))
+    gp, gi = idx.graph_csr()
+    ns = min(len(q), args.cpu_queries)
+    t0 = time.perf_counter()
+    res = O.search(x, forest, gp, gi, q[:ns], k=10, epochs=point[0], init_num=point[1], extend_to=point[2],
+                   trees=SEARCH_TREES, mode=O.OMP, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": round(ns / dt, 1), "unit": "queries/s", "cores": cores, "kind": "port",
+            "sample": "%d of %d queries, same trees/graph/operating point, OpenMP nnexp restatement" % (ns, len(q)),
+            "recall@10": round(recall(res, gt[:ns]), 4)}
+
+
+# ------------------------------------------------------------------------------ reference arm
+def run_reference(args):
+    ws, rank = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    x, q = make_data(args.n, args.nq)
+    p = O.make_params(K=GRAPH["K"], S=GRAPH["S"], L=GRAPH["L"], check_k=GRAPH["check"], epochs=GRAPH["epochs"],
+                      trees=GRAPH["trees"], merge_level=GRAPH["merge_level"])
+    t0 = time.perf_counter()
+    rc, gs, _, _ = O.build_graph(x, p, O.OMP)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    forest = O.Forest.build(x, SEARCH_TREES, mode=O.OMP)
+    trees_s = time.perf_counter() - t0
+    gp, gi = O.graph_csr_from_dense(gs)
+    ns = min(len(q), args.cpu_queries)
+    point = LADDER[5] if args.point is None else tuple(args.point)
+
+    def step(lo):
+        qs = q[lo:lo + ns]
+        return O.search(x, forest, gp, gi, qs, k=10, epochs=point[0], init_num=point[1], extend_to=point[2],
+                        trees=SEARCH_TREES, mode=O.OMP, threads=cores)
+
+    for w in range(args.warmup):
+        step(0)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        step((s * ns) % max(1, len(q) - ns + 1))
+    dt = time.perf_counter() - t0
+    value = ns * args.steps / dt
+    line = {"metric": METRIC, "impl": "reference", "value": round(value, 1), "unit": "queries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded integer-valued Gaussian mixture)",
+            "config": {"workload": "1M x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), "
+                                   "16 search trees, 10k queries, k=10",
+                       "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2]}},
+            "build": {"graph_build_s": round(build_s, 3), "search_trees16_s": round(trees_s, 3), "status": rc},
+            "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": cores, "kind": "port",
+                             "sample": "%d queries per step; index built by the OpenMP restatement of the "
+                                       "reference on the same host" % ns},
+            "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--nq", type=int, default=10_000)
+    ap.add_argument("--cpu-queries", type=int, default=1000)
+    ap.add_argument("--point", type=int, nargs=3, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -43,7 +43,8 @@ class BuildStats(C.Structure):
 
 
 class SearchStats(C.Structure):
-    _fields_ = [("device_ms", C.c_double), ("distance_evals", C.c_uint64), ("queries", C.c_uint64)]
+    _fields_ = [("device_ms", C.c_double), ("distance_evals", C.c_uint64), ("queries", C.c_uint64),
+                ("expanded_nodes", C.c_uint64)]
 
 
 class HostState(C.Structure):
@@ -97,6 +98,7 @@ def lib():
         "efg_index_create_device": (i32, [vp, u64, u32, u64, C.POINTER(BuildParams), C.POINTER(vp)]),
         "efg_index_destroy": (None, [vp]),
         "efg_build_trees": (i32, [vp]),
+        "efg_build_trees_count": (i32, [vp, u32]),
         "efg_build_graph": (i32, [vp]),
         "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
         "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
@@ -173,8 +175,11 @@ class Index:
     def build_index(self) -> None:
         _check(lib().efg_build_graph(self._h))
 
-    def build_trees(self) -> None:
-        _check(lib().efg_build_trees(self._h))
+    def build_trees(self, ntrees: int | None = None) -> None:
+        if ntrees is None:
+            _check(lib().efg_build_trees(self._h))
+        else:
+            _check(lib().efg_build_trees_count(self._h, ntrees))
 
     def build_stats(self) -> BuildStats:
         s = BuildStats()

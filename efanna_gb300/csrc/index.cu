@@ -299,6 +299,7 @@ void efg_index_destroy(efg_index* idx) {
   idx->q_buf.release();
   idx->out_buf.release();
   idx->eval_counter.release();
+  idx->ht_scratch.release();
   if (idx->d_base) cudaFree(idx->d_base);
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;
@@ -307,6 +308,14 @@ void efg_index_destroy(efg_index* idx) {
 int efg_build_trees(efg_index* idx) {
   if (!idx) return fail(EFG_ERR_ARG, "null index");
   return build_forest(idx, idx->bp.trees);
+}
+
+int efg_build_trees_count(efg_index* idx, uint32_t ntrees) {
+  if (!idx) return fail(EFG_ERR_ARG, "null index");
+  if (ntrees < 1 || ntrees > 1024) return fail(EFG_ERR_ARG, "trees must be in [1, 1024]");
+  EFG_TRY(build_forest(idx, ntrees));
+  idx->sp.search_trees = (int)ntrees;
+  return EFG_OK;
 }
 
 int efg_build_graph(efg_index* idx) {

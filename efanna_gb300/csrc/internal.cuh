@@ -96,6 +96,7 @@ struct efg_index {
   efg::DevBuf<float> q_buf;
   efg::DevBuf<int32_t> out_buf;
   efg::DevBuf<unsigned long long> eval_counter;
+  efg::DevBuf<uint32_t> ht_scratch;  // per-CTA visited sets when they do not fit in shared memory
 };
 
 namespace efg {

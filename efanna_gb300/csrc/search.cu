@@ -38,6 +38,7 @@ enum : uint32_t { SERR_STACK = 1u, SERR_HASH = 2u };
 struct SearchCfg {
   uint32_t T, lsize, init_num, extend_to, result_size, epochs, k;
   uint32_t ht_bits, keys_cap, nseq;
+  uint32_t ht_global;  // visited set in a per-CTA slice of global scratch instead of shared memory
   uint64_t seed;
 };
 
@@ -47,7 +48,7 @@ __device__ __forceinline__ uint32_t ht_slot(uint32_t id, uint32_t bits) { return
 __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t bits, uint32_t id, uint32_t* err) {
   uint32_t mask = (1u << bits) - 1, h = ht_slot(id, bits);
   for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-    uint32_t cur = ht[h];
+    uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
     if (cur == kEmpty) {
       uint32_t prev = atomicCAS(&ht[h], kEmpty, id);
       if (prev == kEmpty) return true;
@@ -61,7 +62,7 @@ __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t bits, uint32_t 
 __device__ __forceinline__ bool ht_contains(const uint32_t* ht, uint32_t bits, uint32_t id) {
   uint32_t mask = (1u << bits) - 1, h = ht_slot(id, bits);
   for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-    uint32_t cur = ht[h];
+    uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
     if (cur == kEmpty) return false;
     if ((cur & ID_MASK) == id) return true;
   }
@@ -71,7 +72,7 @@ __device__ __forceinline__ bool ht_contains(const uint32_t* ht, uint32_t bits, u
 __device__ __forceinline__ bool ht_mark_expanded(uint32_t* ht, uint32_t bits, uint32_t id) {
   uint32_t mask = (1u << bits) - 1, h = ht_slot(id, bits);
   for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-    uint32_t cur = ht[h];
+    uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
     if (cur == kEmpty) return false;
     if ((cur & ID_MASK) == id) return (atomicOr(&ht[h], EXPANDED) & EXPANDED) == 0;
   }
@@ -168,24 +169,26 @@ __global__ void __launch_bounds__(S_THREADS) nnexp_kernel(
     const float* __restrict__ base, uint64_t n, uint32_t dim, uint32_t ld, const DNode* __restrict__ nodes,
     const int32_t* __restrict__ roots, const uint32_t* __restrict__ leaves, const uint64_t* __restrict__ gptr,
     const uint32_t* __restrict__ gids, const float* __restrict__ queries, uint64_t nq, uint64_t qld, SearchCfg cfg,
-    int32_t* __restrict__ out, unsigned long long* __restrict__ stats) {
+    int32_t* __restrict__ out, unsigned long long* __restrict__ stats, uint32_t* __restrict__ ht_scratch) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t ld4 = ld >> 2;
   float4* qv = reinterpret_cast<float4*>(smem);
   uint64_t* keys = reinterpret_cast<uint64_t*>(qv + ld4);                  // keys_cap
   uint64_t* chunk = keys + cfg.keys_cap;                                    // S_CHUNK
-  uint32_t* ht = reinterpret_cast<uint32_t*>(chunk + S_CHUNK);             // 1 << ht_bits
-  uint32_t* lstart = ht + (1u << cfg.ht_bits);                             // nseq
+  uint32_t* ht_smem = reinterpret_cast<uint32_t*>(chunk + S_CHUNK);        // 1 << ht_bits (if in smem)
+  uint32_t* ht = cfg.ht_global ? ht_scratch + ((uint64_t)blockIdx.x << cfg.ht_bits) : ht_smem;
+  uint32_t* lstart = ht_smem + (cfg.ht_global ? 0u : (1u << cfg.ht_bits));  // nseq
   uint32_t* lend = lstart + cfg.nseq;                                       // nseq
   uint32_t* seqoff = lend + cfg.nseq;                                       // nseq + 1
   uint8_t* firstflag = reinterpret_cast<uint8_t*>(seqoff + cfg.nseq + 1);  // S_CHUNK
   __shared__ uint32_t warp_tot[S_WARPS];
-  __shared__ uint32_t s_p, s_m, s_err, s_total;
+  __shared__ uint32_t s_p, s_m, s_err, s_total, s_exp;
   __shared__ uint32_t lcount[256];
 
   const uint32_t tid = threadIdx.x;
   const uint32_t ht_size = 1u << cfg.ht_bits;
   unsigned long long evals = 0;
+  if (threadIdx.x == 0) s_exp = 0;
 
   for (uint64_t qi = blockIdx.x; qi < nq; qi += gridDim.x) {
     const float* qrow = queries + qi * qld;
@@ -360,6 +363,7 @@ __global__ void __launch_bounds__(S_THREADS) nnexp_kernel(
         if (kj == ~0ULL) continue;
         uint32_t id = (uint32_t)kj;
         if (!ht_mark_expanded(ht, cfg.ht_bits, id)) continue;
+        atomicAdd(&s_exp, 1u);
         for (uint64_t e = gptr[id], ee = gptr[id + 1]; e < ee; ++e) {
           uint32_t nb = gids[e];
           if (ht_insert(ht, cfg.ht_bits, nb, &s_err)) {
@@ -387,7 +391,10 @@ __global__ void __launch_bounds__(S_THREADS) nnexp_kernel(
     if (tid == 0 && s_err) atomicOr(reinterpret_cast<unsigned int*>(stats + 1), s_err);
     __syncthreads();
   }
-  if (tid == 0) atomicAdd(stats, evals);
+  if (tid == 0) {
+    atomicAdd(stats, evals);
+    atomicAdd(stats + 2, (unsigned long long)s_exp);
+  }
 }
 
 int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
@@ -424,22 +431,26 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
   cfg.keys_cap = next_pow2((uint32_t)std::min<uint64_t>(keys_need, 1u << 20));
   uint64_t visited = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * grow;
   uint32_t bits = 10;
-  while ((1ull << bits) < visited + visited / 2 + 64 && bits < 16) ++bits;
+  while ((1ull << bits) < visited + visited / 2 + 64 && bits < 24) ++bits;
   cfg.ht_bits = bits;
-  size_t smem = (size_t)(idx->ld / 4) * 16 + (size_t)cfg.keys_cap * 8 + S_CHUNK * 8 + ((size_t)1 << bits) * 4 +
-                (size_t)cfg.nseq * 12 + 4 + S_CHUNK;
+  size_t smem_rest = (size_t)(idx->ld / 4) * 16 + (size_t)cfg.keys_cap * 8 + S_CHUNK * 8 + (size_t)cfg.nseq * 12 + 4 +
+                     S_CHUNK;
+  size_t ht_bytes = ((size_t)1 << bits) * 4;
+  cfg.ht_global = smem_rest + ht_bytes > 200 * 1024;
+  size_t smem = smem_rest + (cfg.ht_global ? 0 : ht_bytes);
   if (smem > 220 * 1024)
     return fail(EFG_ERR_ARG, "search parameters need " + std::to_string(smem) +
                                  " bytes of shared memory per query (pool/extend/degree too large)");
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   EFG_CUDA(cudaFuncSetAttribute(nnexp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  EFG_TRY(idx->eval_counter.reserve(2));
-  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 16, s));
+  EFG_TRY(idx->eval_counter.reserve(3));
+  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 24, s));
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nnexp_kernel, S_THREADS, smem);
-  uint64_t grid = std::min<uint64_t>(nq, (uint64_t)sms * std::max(1, per_sm) * 4);
+  uint64_t grid = std::min<uint64_t>(nq, (uint64_t)sms * std::max(1, per_sm) * (cfg.ht_global ? 1 : 4));
+  if (cfg.ht_global) EFG_TRY(idx->ht_scratch.reserve(grid << bits));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -447,7 +458,7 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
   const Forest& F = idx->forest;
   nnexp_kernel<<<(unsigned)grid, S_THREADS, smem, s>>>(idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.d_roots.p,
                                                        F.leaves.p, idx->graph.ptr.p, idx->graph.ids.p, d_q, nq, qld,
-                                                       cfg, d_out, idx->eval_counter.p);
+                                                       cfg, d_out, idx->eval_counter.p, idx->ht_scratch.p);
   cudaError_t le = cudaGetLastError();
   cudaEventRecord(e1, s);
   if (le != cudaSuccess) {
@@ -456,14 +467,15 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
     return fail(EFG_ERR_CUDA, std::string("nnexp launch: ") + cudaGetErrorString(le));
   }
   if (count_evals) {
-    unsigned long long h[2];
-    EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 16, cudaMemcpyDeviceToHost, s));
+    unsigned long long h[3];
+    EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 24, cudaMemcpyDeviceToHost, s));
     EFG_CUDA(cudaStreamSynchronize(s));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     idx->sstats.device_ms = ms;
     idx->sstats.distance_evals = h[0];
     idx->sstats.queries = nq;
+    idx->sstats.expanded_nodes = h[2];
     if (h[1] & SERR_STACK) return fail(EFG_ERR_DEVICE_LIMIT, "tree deeper than the search stack");
     if (h[1] & SERR_HASH) return fail(EFG_ERR_DEVICE_LIMIT, "visited set overflow");
   }

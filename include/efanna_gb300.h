@@ -70,6 +70,7 @@ typedef struct efg_search_stats {
   double device_ms;         /* kernel time of the last search call                             */
   uint64_t distance_evals;  /* query-to-base distances computed by the last search call         */
   uint64_t queries;
+  uint64_t expanded_nodes;  /* graph rows read by the expansion epochs of the last search call  */
 } efg_search_stats;
 
 typedef struct efg_index efg_index;
@@ -88,6 +89,9 @@ void efg_index_destroy(efg_index* idx);
 
 /* FIndex::buildTrees — efanna.hpp:28-31, kdtreeub_index.hpp:1192-1276. */
 int efg_build_trees(efg_index* idx);
+/* buildTrees with an explicit tree count: the trees a KDTreeUbIndexParams(true, ntrees) index
+ * over the same data would build (samples/efanna_index_buildtrees.cc:42-46); the graph is kept. */
+int efg_build_trees_count(efg_index* idx, uint32_t ntrees);
 /* FIndex::buildIndex — efanna.hpp:24-27, kdtreeub_index.hpp:92-113 (initGraph + refineGraph). */
 int efg_build_graph(efg_index* idx);
 int efg_get_build_stats(const efg_index* idx, efg_build_stats* out);

@@ -20,6 +20,7 @@
 //
 // Reference files cited below are paths inside the ZJULearning/efanna project.
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -38,7 +39,7 @@
 
 namespace orc {
 
-enum { MODE_SEQ = 0, MODE_CANON = 1 };
+enum { MODE_SEQ = 0, MODE_CANON = 1, MODE_OMP = 2 };
 
 // ----------------------------------------------------------------------------------------------
 // Squared L2 distances.
@@ -54,6 +55,14 @@ static float l2_avx(const float* a, const float* b, size_t size) {
   unsigned DD = D - DR;
   float sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   auto lane = [&](unsigned base) {
+    if (base + 8 <= size) {  // full block: no padding involved
+      for (unsigned k = 0; k < 8; ++k) {
+        float t = a[base + k] - b[base + k];
+        t = t * t;
+        sum[k] = sum[k] + t;
+      }
+      return;
+    }
     for (unsigned k = 0; k < 8; ++k) {
       unsigned idx = base + k;
       float x = idx < size ? a[idx] : 0.0f;
@@ -95,7 +104,7 @@ struct Data {
   size_t n, d, ld;
   int mode;
   const float* row(size_t i) const { return p + i * ld; }
-  float distq(const float* a, const float* b) const { return mode == 0 ? l2_avx(a, b, d) : l2_scalar(a, b, d); }
+  float distq(const float* a, const float* b) const { return mode != 1 ? l2_avx(a, b, d) : l2_scalar(a, b, d); }
   float dist(size_t i, size_t j) const { return distq(row(i), row(j)); }
 };
 
@@ -948,6 +957,273 @@ static int init_graph(const Data& X, const Forest& F, const Params& p, int mode,
   return 0;
 }
 
+// ----------------------------------------------------------------------------------------------
+// Multi-threaded restatement (ORC_OMP): the reference's OpenMP build with its parallel loops and
+// per-node spin locks, used only as the CPU timing baseline (its output depends on thread timing,
+// as the reference's does).  kdtreeub_index.hpp:1311-1423, base_index.hpp:328-437.
+// ----------------------------------------------------------------------------------------------
+struct Spin {
+  std::atomic_flag f = ATOMIC_FLAG_INIT;
+  void lock() { while (f.test_and_set(std::memory_order_acquire)) { } }
+  void unlock() { f.clear(std::memory_order_release); }
+};
+static inline int thread_id() {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+static void dfs_build_local(const Data& X, std::vector<Node>& sub, int32_t node, std::mt19937& rng,
+                            unsigned* indices, unsigned count, unsigned offset, unsigned tns) {
+  dfs_build(X, sub, node, rng, indices, count, offset, tns);
+}
+
+static void build_forest_omp(const Data& X, unsigned T, unsigned S, unsigned tns, Forest& F) {
+  unsigned N = (unsigned)X.n;
+  F.n = X.n;
+  F.dim = X.d;
+  F.nodes.assign(T, {});
+  F.roots.assign(T, 0);
+  F.leaves.assign(T, {});
+  std::vector<std::pair<unsigned, int32_t>> active, next;
+  for (unsigned t = 0; t < T; ++t) {
+    F.roots[t] = new_node(F.nodes[t], -1, 0, N);
+    active.push_back({t, F.roots[t]});
+    F.leaves[t].resize(N);
+  }
+#pragma omp parallel for
+  for (int t = 0; t < (int)T; ++t) {
+    std::vector<unsigned>& ids = F.leaves[t];
+    for (unsigned i = 0; i < N; ++i) ids[i] = i;
+    std::random_shuffle(ids.begin(), ids.end());
+  }
+  struct Split { unsigned mid, dim; float val; };
+  while (!active.empty() && active.size() < 1100) {
+    std::vector<Split> sp(active.size());
+#pragma omp parallel for
+    for (long a = 0; a < (long)active.size(); ++a) {
+      std::mt19937 rng(1998 ^ thread_id());
+      const Node& nd = F.nodes[active[a].first][active[a].second];
+      mean_split_seq(X, rng, &F.leaves[active[a].first][0] + nd.start, (unsigned)(nd.end - nd.start), sp[a].mid,
+                     sp[a].dim, sp[a].val);
+    }
+    next.clear();
+    for (size_t a = 0; a < active.size(); ++a) {
+      unsigned t = active[a].first;
+      int32_t ni = active[a].second;
+      std::vector<Node>& nodes = F.nodes[t];
+      uint64_t s = nodes[ni].start, e = nodes[ni].end;
+      nodes[ni].div_dim = (int)sp[a].dim;
+      nodes[ni].div_val = sp[a].val;
+      int32_t l = new_node(nodes, 0, s, s + sp[a].mid);
+      int32_t r = new_node(nodes, 0, s + sp[a].mid, e);
+      nodes[ni].left = l;
+      nodes[ni].right = r;
+      if (sp[a].mid > S) next.push_back({t, l});
+      if (e - (s + sp[a].mid) > S) next.push_back({t, r});
+    }
+    active.swap(next);
+  }
+  std::vector<std::vector<Node>> subs(active.size());
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long a = 0; a < (long)active.size(); ++a) {
+    std::mt19937 rng(1998 ^ thread_id());
+    const Node& nd = F.nodes[active[a].first][active[a].second];
+    std::vector<Node>& sub = subs[a];
+    sub.push_back(nd);
+    dfs_build_local(X, sub, 0, rng, &F.leaves[active[a].first][0] + nd.start, (unsigned)(nd.end - nd.start),
+                    (unsigned)nd.start, tns);
+  }
+  for (size_t a = 0; a < active.size(); ++a) {  // splice the subtrees in
+    std::vector<Node>& nodes = F.nodes[active[a].first];
+    int32_t base = (int32_t)nodes.size() - 1;
+    std::vector<Node>& sub = subs[a];
+    for (size_t j = 0; j < sub.size(); ++j) {
+      Node nd = sub[j];
+      if (nd.left >= 0) {
+        nd.left = nd.left == 0 ? active[a].second : nd.left + base;
+        nd.right = nd.right == 0 ? active[a].second : nd.right + base;
+      }
+      if (j == 0) nodes[active[a].second] = nd;
+      else nodes.push_back(nd);
+    }
+  }
+}
+
+static void merge_subgraphs_omp(const Forest& F, const Data& X, unsigned t, int32_t ni, const Params& p,
+                                std::vector<CandHeap>& knn, State& st, std::vector<Spin>& locks) {
+  const Node& nd = F.nodes[t][ni];
+  if (!(nd.left >= 0 && nd.right >= 0)) return;
+  merge_subgraphs_omp(F, X, t, nd.left, p, knn, st, locks);
+  merge_subgraphs_omp(F, X, t, nd.right, p, knn, st, locks);
+  const Node& L = F.nodes[t][nd.left];
+  const Node& R = F.nodes[t][nd.right];
+  size_t numL = L.end - L.start, numR = R.end - R.start;
+  int32_t root = numL < numR ? nd.right : nd.left;
+  size_t start = numL < numR ? L.start : R.start, end = numL < numR ? L.end : R.end;
+  for (; start < end; start++) {
+    size_t fid = F.leaves[t][start];
+    int32_t leaf = search_to_leaf(F, X, t, root, fid);
+    const Node& lf = F.nodes[t][leaf];
+    for (size_t i = lf.start; i < lf.end; i++) {
+      size_t tf = F.leaves[t][i];
+      float dist = X.dist(tf, fid);
+      auto offer = [&](size_t tgt, size_t cand) {
+        locks[tgt].lock();
+        CandHeap& h = knn[tgt];
+        if (h.size() < p.S || dist < h.begin()->distance) {
+          h.insert(Cand{cand, dist});
+          if (h.size() > p.S) h.erase(h.begin());
+        } else if (st.nn_new[tgt].size() < p.S * 2) {
+          st.nn_new[tgt].push_back((uint32_t)cand);
+        }
+        locks[tgt].unlock();
+      };
+      offer(tf, fid);
+      offer(fid, tf);
+    }
+  }
+}
+
+static int init_graph_omp(const Data& X, const Forest& F, const Params& p, State& st, std::vector<Spin>& locks,
+                          int* max_depth) {
+  size_t N = X.n;
+  st.init(N, p.L);
+  std::vector<std::pair<int32_t, unsigned>> ml_nodes;
+  bool err = false;
+  int maxd = 0x0fffffff;
+  for (unsigned t = 0; t < p.trees_build; ++t)
+    merge_level_nodes(F, t, F.roots[t], 0, (int)p.merge_level, ml_nodes, err, maxd);
+  if (max_depth) *max_depth = maxd;
+  if (err) return 3;
+  std::vector<CandHeap> knn(N);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long i = 0; i < (long)ml_nodes.size(); ++i)
+    merge_subgraphs_omp(F, X, ml_nodes[i].second, ml_nodes[i].first, p, knn, st, locks);
+#pragma omp parallel
+  {
+    std::mt19937 rng(1998 ^ thread_id());
+    std::vector<unsigned> random(p.S + 1);
+#pragma omp for
+    for (long nn = 0; nn < (long)N; ++nn) {
+      std::vector<uint32_t>& nw = st.nn_new[nn];
+      if (nw.size() < p.S * 2) {
+        nw.resize(p.S * 2);
+        gen_random(rng, &nw[0], (unsigned)nw.size(), (unsigned)N);
+      }
+      gen_random(rng, &random[0], (unsigned)random.size(), (unsigned)N);
+      st.L[nn] = p.S;
+      st.Range[nn] = p.S;
+      while (knn[nn].size() < p.S) {
+        unsigned rid = rng() % (unsigned)N;
+        knn[nn].insert(Cand{rid, X.dist(nn, rid)});
+      }
+      Point* pool = st.row(nn);
+      auto it = knn[nn].rbegin();
+      for (unsigned l = 0; l < st.L[nn]; ++l, ++it) {
+        pool[l] = Point{(uint32_t)it->row_id, it->distance, true};
+        nw[l] = (uint32_t)it->row_id;
+      }
+      std::sort(pool, pool + st.L[nn], [](const Point& a, const Point& b) { return a.dist < b.dist; });
+    }
+  }
+  return 0;
+}
+
+static uint64_t join_omp(const Data& X, State& st, const Params& p, std::vector<Spin>& locks) {
+  uint64_t cc = 0;
+  auto ins = [&](size_t t, uint32_t id, float dist) -> unsigned {
+    if (dist > st.radius[t]) return st.P;  // unlocked read, as Neighbor::insert
+    locks[t].lock();
+    unsigned r = nb_insert(st, t, id, dist);
+    locks[t].unlock();
+    return r;
+  };
+#pragma omp parallel for schedule(dynamic, 100) reduction(+ : cc)
+  for (long i = 0; i < (long)st.n; ++i) {
+    size_t uu = 0;
+    st.found[i] = 0;
+    const std::vector<uint32_t>& nw = st.nn_new[i];
+    const std::vector<uint32_t>& od = st.nn_old[i];
+    auto cb = [&](unsigned a, unsigned b) {
+      float dist = X.dist(a, b);
+      ++cc;
+      unsigned r = ins(a, b, dist);
+      if (r < p.check_k) ++uu;
+      ins(b, a, dist);
+      if (r < p.check_k) ++uu;
+    };
+    for (unsigned a : nw) {
+      for (unsigned b : nw)
+        if (a < b) cb(a, b);
+      for (unsigned b : od) cb(a, b);
+    }
+    st.found[i] = uu > 0;
+  }
+  return cc;
+}
+
+static void update_omp(State& st, const Params& p, std::vector<Spin>& locks) {
+  size_t n = st.n;
+  std::vector<std::vector<uint32_t>> rnn_new(n), rnn_old(n);
+  for (size_t i = 0; i < n; ++i) {
+    st.nn_new[i].clear();
+    st.nn_old[i].clear();
+    st.radius[i] = st.row(i)[st.P - 1].dist;
+  }
+#pragma omp parallel for
+  for (long i = 0; i < (long)n; ++i) {
+    Point* pool = st.row(i);
+    if (st.found[i]) {
+      unsigned maxl = st.Range[i] + p.S < st.L[i] ? st.Range[i] + p.S : st.L[i];
+      unsigned c = 0, l = 0;
+      while ((l < maxl) && (c < p.S)) {
+        if (pool[l].flag) ++c;
+        ++l;
+      }
+      st.Range[i] = l;
+    }
+    st.radiusM[i] = pool[st.Range[i] - 1].dist;
+  }
+#pragma omp parallel for
+  for (long nn = 0; nn < (long)n; ++nn) {
+    Point* pool = st.row(nn);
+    for (unsigned l = 0; l < st.Range[nn]; ++l) {
+      Point& e = pool[l];
+      if (e.flag) {
+        st.nn_new[nn].push_back(e.id);
+        if (e.dist > st.radiusM[e.id]) {
+          locks[e.id].lock();
+          rnn_new[e.id].push_back((uint32_t)nn);
+          locks[e.id].unlock();
+        }
+        e.flag = false;
+      } else {
+        st.nn_old[nn].push_back(e.id);
+        if (e.dist > st.radiusM[e.id]) {
+          locks[e.id].lock();
+          rnn_old[e.id].push_back((uint32_t)nn);
+          locks[e.id].unlock();
+        }
+      }
+    }
+  }
+  unsigned cap = p.reverse_cap;
+  for (size_t i = 0; i < n; ++i) {
+    for (int which = 0; which < 2; ++which) {
+      std::vector<uint32_t>& R = which == 0 ? rnn_new[i] : rnn_old[i];
+      if (cap && R.size() > cap) {
+        std::random_shuffle(R.begin(), R.end());
+        R.resize(cap);
+      }
+      std::vector<uint32_t>& dst = which == 0 ? st.nn_new[i] : st.nn_old[i];
+      dst.insert(dst.end(), R.begin(), R.end());
+    }
+  }
+}
+
 static void export_graph(State& st, uint32_t K, uint32_t* gs) {
   for (size_t i = 0; i < st.n; ++i)
     for (uint32_t j = 0; j < K; ++j) gs[i * K + j] = st.row(i)[j].id;
@@ -1096,6 +1372,9 @@ void* orc_forest_build(const float* data, uint64_t n, uint32_t d, uint64_t ld, u
   if (mode == MODE_SEQ) {
     srand(1);
     build_forest_seq(X, trees, S, tns, *F);
+  } else if (mode == MODE_OMP) {
+    srand(1);
+    build_forest_omp(X, trees, S, tns, *F);
   } else {
     build_forest_canon(X, trees, S, tns, seed, *F);
   }
@@ -1114,15 +1393,19 @@ int orc_build_graph(const float* data, uint64_t n, uint32_t d, uint64_t ld, cons
   Data X{data, n, d, ld, mode};
   Params p = to_params(pp);
   Forest* F = new Forest();
+  std::vector<Spin> locks(mode == MODE_OMP ? n : 0);
   if (mode == MODE_SEQ) {
     srand(1);
     build_forest_seq(X, p.trees, p.S, p.tns, *F);
+  } else if (mode == MODE_OMP) {
+    srand(1);
+    build_forest_omp(X, p.trees, p.S, p.tns, *F);
   } else {
     build_forest_canon(X, p.trees, p.S, p.tns, p.seed, *F);
   }
   State st;
   int maxd = 0;
-  int rc = init_graph(X, *F, p, mode, st, &maxd);
+  int rc = mode == MODE_OMP ? init_graph_omp(X, *F, p, st, locks, &maxd) : init_graph(X, *F, p, mode, st, &maxd);
   if (stats) stats[0] = stats[1] = 0;
   if (rc != 0) {
     if (stats) stats[1] = (uint64_t)(maxd - 1);
@@ -1132,8 +1415,13 @@ int orc_build_graph(const float* data, uint64_t n, uint32_t d, uint64_t ld, cons
   }
   uint64_t cc = 0;
   for (uint32_t it = 0; it < p.epochs; ++it) {
-    cc += mode == MODE_SEQ ? join_seq(X, st, p) : join_canon(X, st, p);
-    update(st, p, mode, it);
+    if (mode == MODE_OMP) {
+      cc += join_omp(X, st, p, locks);
+      update_omp(st, p, locks);
+    } else {
+      cc += mode == MODE_SEQ ? join_seq(X, st, p) : join_canon(X, st, p);
+      update(st, p, mode, it);
+    }
   }
   export_graph(st, p.K, gs_out);
   if (stats) stats[0] = cc;
@@ -1213,7 +1501,7 @@ int orc_search(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* for
   SearchArgs a{epochs, init_num, extend_to, search_trees, k};
   if (mode == MODE_SEQ) srand(1);
 #ifdef _OPENMP
-  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;
+  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;  // sequential fill uses std::rand()
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
 #endif
   for (long long i = 0; i < (long long)nq; ++i)

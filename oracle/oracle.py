@@ -14,7 +14,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-SEQ, CANON = 0, 1
+SEQ, CANON, OMP = 0, 1, 2
 
 
 class Params(C.Structure):

@@ -16,6 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libefanna_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "efg_cli.cc")
+CLI = os.path.join(HERE, "cli", "efg_cli")
 SOURCES = ["index.cu", "distance.cu", "search.cu", "trees.cu", "nndescent.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -61,6 +63,21 @@ def build(verbose: bool = False) -> str:
     return LIB
 
 
+def build_cli() -> str:
+    """The reference-shaped command-line tools, linked against the library (host C++ only)."""
+    lib = build()
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC), os.path.getmtime(lib)):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++11", "-O2", CLI_SRC, "-o", CLI,
+           "-I" + os.path.join(ROOT, "include", "efanna_gb300"), "-L" + HERE, "-lefanna_gb300",
+           "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s%s" % (r.stdout, r.stderr))
+    return CLI
+
+
 if __name__ == "__main__":
     build(verbose=True)
+    build_cli()
     sys.exit(0)

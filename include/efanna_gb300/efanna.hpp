@@ -1,0 +1,288 @@
+// Drop-in replacement for the reference's efanna.hpp (ZJULearning/efanna): the same namespace,
+// classes and signatures -- FIndex<float>, KDTreeUbIndexParams, IndexParams, SearchParams,
+// Matrix<T>, Distance<T> and the L2Distance* tags -- over the efanna_gb300 C ABI
+// (include/efanna_gb300.h), so code written against the reference compiles unchanged with
+// `-I include/efanna_gb300` and links with `-lefanna_gb300`.
+//
+// Reference interfaces mirrored:
+//   FIndex                efanna.hpp:9-75
+//   IndexParams / SearchParams / init_algorithm / ValueType / ExtraParamsMap
+//                         general/params.hpp:7-42
+//   KDTreeUbIndexParams   algorithm/kdtreeub_index.hpp:14-35
+//   Matrix                general/matrix.hpp:12-72
+//   Distance, L2Distance, L2DistanceSSE, L2DistanceAVX, L2DistanceAVXr4
+//                         general/distance.hpp:46-379 (here plain C++; the GPU computes the
+//                         squared L2 itself, the object only names the metric)
+// Error behaviour follows the reference: unopenable files print "open file error" and exit with
+// the reference's codes, an over-deep merge level prints the reference's message and leaves no
+// graph, too many search trees prints "wrong tree number"; other failures throw
+// std::runtime_error with efg_last_error().
+#ifndef EFANNA_GB300_EFANNA_HPP
+#define EFANNA_GB300_EFANNA_HPP
+
+#include <cstddef>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+#include <algorithm>
+
+#include "../efanna_gb300.h"
+
+#ifdef __GNUC__
+#ifdef __AVX__
+#define KGRAPH_MATRIX_ALIGN 32
+#else
+#ifdef __SSE2__
+#define KGRAPH_MATRIX_ALIGN 16
+#else
+#define KGRAPH_MATRIX_ALIGN 4
+#endif
+#endif
+#endif
+
+namespace efanna {
+
+// ---- distances (general/distance.hpp) ----------------------------------------------------------
+template <typename T>
+struct Candidate {
+  size_t row_id;
+  T distance;
+  Candidate(const size_t row_id, const T distance) : row_id(row_id), distance(distance) {}
+  bool operator>(const Candidate& rhs) const {
+    if (this->distance == rhs.distance) return this->row_id > rhs.row_id;
+    return this->distance > rhs.distance;
+  }
+  bool operator<(const Candidate& rhs) const {
+    if (this->distance == rhs.distance) return this->row_id < rhs.row_id;
+    return this->distance < rhs.distance;
+  }
+};
+
+template <typename T>
+class Distance {
+ public:
+  virtual T compare(const T* a, const T* b, size_t length) const = 0;
+  virtual T norm(const T* a, size_t length) const = 0;
+  virtual T dot(const T* a, const T* b, size_t length) const = 0;
+  virtual ~Distance() {}
+};
+
+// Squared L2 on the host (used by Matrix::brute_force_search and by callers); the index itself
+// always measures squared L2 on the GPU whichever of these tags it is given.
+template <typename T>
+class L2Distance : public Distance<T> {
+ public:
+  T compare(const T* a, const T* b, size_t size) const {
+    T r = T();
+    for (size_t i = 0; i < size; ++i) {
+      T d = a[i] - b[i];
+      r += d * d;
+    }
+    return r;
+  }
+  T norm(const T* a, size_t size) const {
+    T r = T();
+    for (size_t i = 0; i < size; ++i) r += a[i] * a[i];
+    return r;
+  }
+  T dot(const T* a, const T* b, size_t size) const {
+    T r = T();
+    for (size_t i = 0; i < size; ++i) r += a[i] * b[i];
+    return r;
+  }
+};
+template <typename T>
+class L2DistanceSSE : public L2Distance<T> {};
+template <typename T>
+class L2DistanceAVX : public L2Distance<T> {};
+template <typename T>
+class L2DistanceAVXr4 : public L2Distance<T> {};
+
+// ---- parameters (general/params.hpp, algorithm/kdtreeub_index.hpp:14-35) ------------------------
+enum init_algorithm { KDTREE_UB, HASHING };
+union ValueType {
+  int int_val;
+  float float_val;
+  char* str_pt;
+};
+typedef std::map<std::string, ValueType> ExtraParamsMap;
+struct IndexParams {
+  init_algorithm init_index_type;
+  size_t K;
+  size_t S;
+  size_t L = 30;
+  size_t TNS = 10;
+  size_t Check_K = 40;
+  int build_epoches;
+  int extend_num;
+  size_t pool_size = 100;
+  size_t init_num = 100;
+  ExtraParamsMap extra_params;
+  bool reverse_nn_used;
+};
+struct SearchParams {
+  int search_init_num;
+  int search_epoches;
+  int search_method;
+  unsigned extend_to;
+  unsigned tree_num;
+  unsigned search_depth;
+};
+struct KDTreeUbIndexParams : public IndexParams {
+  KDTreeUbIndexParams(bool rnn_used, int tree_num_total, int merge_level = 4, int epoches = 4, int check = 25,
+                      int myL = 30, int building_use_k = 10, int tree_num_build = 0, int myS = 10) {
+    reverse_nn_used = rnn_used;
+    init_index_type = KDTREE_UB;
+    K = building_use_k;
+    build_epoches = epoches;
+    S = myS;
+    ValueType v;
+    v.int_val = tree_num_total;
+    extra_params.insert(std::make_pair("trees", v));
+    v.int_val = tree_num_build > 0 ? tree_num_build : tree_num_total;
+    extra_params.insert(std::make_pair("treesb", v));
+    v.int_val = merge_level;
+    extra_params.insert(std::make_pair("ml", v));
+    L = myL;
+    Check_K = check;
+  }
+};
+
+// ---- Matrix (general/matrix.hpp): a non-owning row view with the reference's padding rule -------
+template <typename T>
+class Matrix {
+ public:
+  Matrix(const size_t rows, const size_t cols, const void* data) : rows_(rows), cols_(cols), data_(data) {
+#ifdef __AVX__
+    align_cols_ = (cols + 7) / 8 * 8;
+#else
+#ifdef __SSE2__
+    align_cols_ = (cols + 3) / 4 * 4;
+#else
+    align_cols_ = cols;
+#endif
+#endif
+  }
+  size_t get_cols() const { return cols_; }
+  size_t get_rows() const { return rows_; }
+  size_t get_stride() const { return align_cols_; }
+  const T* data() const { return reinterpret_cast<const T*>(data_); }
+  const T* get_row(const size_t index) const {
+    if (index >= rows_) throw std::runtime_error("index out of range");
+    return reinterpret_cast<const T*>(data_) + align_cols_ * index;
+  }
+  std::vector<std::pair<T, size_t> > brute_force_search(size_t idx, size_t k, Distance<T>* distance) const {
+    std::vector<std::pair<T, size_t> > result;
+    for (size_t i = 0; i < rows_; i++) result.push_back(std::make_pair(distance->compare(get_row(i), get_row(idx), cols_), i));
+    std::partial_sort(result.begin(), result.begin() + k, result.end());
+    result.resize(k);
+    return result;
+  }
+
+ private:
+  size_t rows_, cols_, align_cols_;
+  const void* data_;
+};
+
+// ---- FIndex (efanna.hpp) ------------------------------------------------------------------------
+template <typename DataType>
+class FIndex {
+ public:
+  FIndex(const Matrix<DataType>& features, Distance<DataType>* d, const IndexParams& params)
+      : index_params_(params), distance_(d), idx_(nullptr) {
+    static_assert(sizeof(DataType) == 4, "efanna_gb300 indexes float vectors");
+    if (params.init_index_type != KDTREE_UB)
+      throw std::runtime_error("efanna_gb300 provides the KD-tree (KDTREE_UB) initialisation only");
+    efg_build_params p;
+    efg_default_build_params(&p);
+    p.K = (uint32_t)params.K;
+    p.S = (uint32_t)params.S;
+    p.L = (uint32_t)params.L;
+    p.check_k = (uint32_t)params.Check_K;
+    p.epochs = (uint32_t)params.build_epoches;
+    p.leaf_size = (uint32_t)params.TNS;
+    ExtraParamsMap::const_iterator it = params.extra_params.find("trees");
+    p.trees = it != params.extra_params.end() ? (uint32_t)it->second.int_val : 4;
+    it = params.extra_params.find("treesb");
+    p.trees_build = it != params.extra_params.end() ? (uint32_t)it->second.int_val : p.trees;
+    it = params.extra_params.find("ml");
+    p.merge_level = it != params.extra_params.end() ? (uint32_t)it->second.int_val : 0;
+    check(efg_index_create(reinterpret_cast<const float*>(features.data()), features.get_rows(),
+                           (uint32_t)features.get_cols(), features.get_stride(), &p, &idx_));
+  }
+  virtual ~FIndex() { efg_index_destroy(idx_); }
+
+  void buildIndex() {
+    int rc = efg_build_graph(idx_);
+    if (rc == EFG_ERR_MERGE_LEVEL) {
+      efg_build_stats s;
+      efg_get_build_stats(idx_, &s);
+      std::cout << "merge level deeper than tree, max merge deepth is" << s.max_merge_depth << std::endl;
+      return;
+    }
+    check(rc);
+  }
+  void buildTrees() { check(efg_build_trees(idx_)); }
+  void knnSearch(int k, const Matrix<DataType>& query) {
+    std::vector<int32_t> out((size_t)query.get_rows() * (size_t)k);
+    int rc = efg_knn_search(idx_, reinterpret_cast<const float*>(query.data()), query.get_rows(),
+                            (uint32_t)query.get_cols(), query.get_stride(), (uint32_t)k, out.data());
+    if (rc == EFG_ERR_TREE_COUNT) {
+      std::cout << "wrong tree number" << std::endl;
+      return;
+    }
+    check(rc);
+  }
+  void saveIndex(char* filename) { file(efg_save_index(idx_, filename), -10086); }
+  void loadIndex(char* filename) { file(efg_load_index(idx_, filename), -10087); }
+  void saveTrees(char* filename) { file(efg_save_trees(idx_, filename), -10086); }
+  void loadTrees(char* filename) { file(efg_load_trees(idx_, filename), -10087); }
+  void saveGraph(char* filename) {
+    int rc = efg_save_graph(idx_, filename);
+    if (rc != EFG_ERR_STATE) file(rc, -10086);  // no graph: the reference writes an empty file
+  }
+  void loadGraph(char* filename) { file(efg_load_graph(idx_, filename), -10087); }
+  void saveResults(char* filename) { file(efg_save_results(idx_, filename), -10086); }
+  void setSearchParams(int epochs, int init_num, int extend_to, int search_trees = 0, int search_lv = -1,
+                       int search_method = 0) {
+    check(efg_set_search_params(idx_, epochs, init_num, extend_to, search_trees, search_lv, search_method));
+  }
+  size_t getGraphSize() { return (size_t)efg_graph_size(idx_); }
+  std::vector<unsigned> getGraphRow(unsigned row_id) {
+    std::vector<unsigned> row;
+    int64_t len = efg_graph_row(idx_, row_id, nullptr, 0);
+    if (len > 0) {
+      row.resize((size_t)len);
+      efg_graph_row(idx_, row_id, reinterpret_cast<uint32_t*>(row.data()), (uint64_t)len);
+    }
+    return row;
+  }
+  void outputVisitBucketNum() {}
+
+ private:
+  static void check(int rc) {
+    if (rc != EFG_OK) throw std::runtime_error(std::string("efanna_gb300: ") + efg_last_error());
+  }
+  static void file(int rc, int exit_code) {
+    if (rc == EFG_ERR_OPEN) {
+      std::cout << "open file error" << std::endl;
+      std::exit(exit_code);
+    }
+    if (rc == EFG_ERR_FORMAT) {
+      std::cout << efg_last_error() << std::endl;
+      std::exit(-11);
+    }
+    check(rc);
+  }
+  IndexParams index_params_;
+  Distance<DataType>* distance_;
+  efg_index* idx_;
+};
+
+}  // namespace efanna
+#endif

@@ -117,6 +117,7 @@ def lib():
         "efg_version": (C.c_char_p, []),
         "efg_l2_pairs": (i32, [vp, u64, u32, u64, vp, vp, u64, vp, vp]),
         "efg_brute_force_knn": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_nnd_init": (i32, [vp, C.POINTER(HostState)]),
         "efg_nnd_iterate": (i32, [vp, C.POINTER(HostState), u32, C.POINTER(C.c_uint64)]),
     }
@@ -280,6 +281,15 @@ def brute_force_knn_device(base_ptr: int, n: int, dim: int, row_stride: int, q_p
     _check(lib().efg_brute_force_knn(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(q_ptr), nq, q_stride, k,
                                      int(exclude_self), first_row, C.c_void_p(ids_ptr),
                                      C.c_void_p(dists_ptr or None), C.c_void_p(stream)))
+
+
+def brute_force_knn_device_noalloc(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int,
+                                   q_stride: int, k: int, ids_ptr: int, dists_ptr: int = 0, exclude_self: bool = False,
+                                   first_row: int = 0, stream: int = 0) -> None:
+    """efg_brute_force_knn_noalloc: the same results with no device allocation (fixed built-in scratch)."""
+    _check(lib().efg_brute_force_knn_noalloc(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(q_ptr), nq,
+                                             q_stride, k, int(exclude_self), first_row, C.c_void_p(ids_ptr),
+                                             C.c_void_p(dists_ptr or None), C.c_void_p(stream)))
 
 
 def version() -> str:

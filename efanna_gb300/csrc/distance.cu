@@ -317,4 +317,41 @@ int brute_force_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, co
   return EFG_OK;
 }
 
+// The same two kernels with caller-provided scratch for the per-(query, chunk) candidate lists:
+// `part` holds part_cap keys; the base is cut into as many chunks as fit (at least one).  Every
+// slot the merge reads is written by bf_chunk_kernel first, so the scratch needs no clearing.
+int brute_force_knn_in(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                       uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                       uint64_t* part, uint64_t part_cap, cudaStream_t s) {
+  if (nq == 0) return EFG_OK;
+  uint32_t K2 = std::min<uint64_t>(k + BF_MARGIN, n);
+  if (nq * K2 > part_cap)
+    return fail(EFG_ERR_ARG, "brute force needs " + std::to_string(nq * K2) + " scratch entries (queries x (k+" +
+                                 std::to_string(BF_MARGIN) + ")); the built-in scratch holds " +
+                                 std::to_string(part_cap));
+  uint64_t qblocks = (nq + BF_QB - 1) / BF_QB;
+  uint64_t want = std::max<uint64_t>(1, (152ull * 8 + qblocks - 1) / qblocks);
+  uint64_t nchunks = std::min<uint64_t>(want, std::max<uint64_t>(1, n / 2048));
+  nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, 4096 / K2));
+  nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, part_cap / (nq * K2)));
+  uint64_t chunk = (n + nchunks - 1) / nchunks;
+  nchunks = (n + chunk - 1) / chunk;
+  uint32_t ld4 = (dim + 3) / 4;
+  size_t smem = (size_t)BF_QB * ld4 * 16 + (size_t)BF_QB * BF_CAP * 8;
+  if (smem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)qblocks, (unsigned)nchunks);
+  bf_chunk_kernel<<<grid, BF_THREADS, smem, s>>>(base, n, dim, ld, q, nq, qld, K2, chunk, exclude_self, first_row,
+                                                 part);
+  EFG_CUDA(cudaGetLastError());
+  uint32_t tot = (uint32_t)(nchunks * K2), p2 = 1;
+  while (p2 < tot) p2 <<= 1;
+  uint32_t wpb = p2 <= 2048 ? 4 : 1;
+  size_t msmem = (size_t)wpb * p2 * 8 + (size_t)wpb * K2 * 8;
+  if (msmem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem));
+  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2,
+                                                                            (uint32_t)nchunks, part, ids, dists);
+  EFG_CUDA(cudaGetLastError());
+  return EFG_OK;
+}
+
 }  // namespace efg

@@ -1,0 +1,73 @@
+// Exact brute-force k-NN that allocates no device memory.
+//
+// efg_brute_force_knn takes the per-(query, chunk) candidate lists it needs between its two
+// kernels from cudaMallocAsync.  Some callers cannot let a library allocate device memory when
+// they call it: a host process whose GPU memory is handed out by its own allocator (a memory
+// pool or a framework's caching allocator that has reserved the device, where a foreign
+// cudaMalloc can fail or fragment what it manages), or a latency-critical loop that must not pay
+// for an allocation and its implicit synchronisation.  efg_brute_force_knn_noalloc serves them:
+// its scratch is a fixed array in this file, compiled into the library, so every GPU that loads
+// the library holds these 16 MiB until the process exits.
+//
+// The array's name in host code is only a host-side stand-in, not a device address; the device
+// address is looked up with cudaGetSymbolAddress once per device, on the first call made with
+// that device current, and cached.  That first call should come before any stream capture.
+// All calls share the one array: calls that overlap on the GPU (concurrent streams, or threads
+// sharing a device) race on it and must be serialised by the caller.  Nothing in it needs to start
+// at zero -- every entry the second kernel reads is written by the first kernel of the same call.
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace efg {
+int brute_force_knn_in(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                       uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                       uint64_t* part, uint64_t part_cap, cudaStream_t s);
+}  // namespace efg
+
+namespace {
+
+constexpr uint64_t kScratchEntries = EFG_BF_NOALLOC_SCRATCH_ENTRIES;  // 2^21 keys x 8 B = 16 MiB
+static __device__ __align__(256) uint64_t g_bf_scratch[kScratchEntries];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+uint64_t* g_dev_ptr[kMaxDevices] = {};
+
+// Device address of g_bf_scratch on the current device (looked up once per device).
+int scratch_address(uint64_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return efg::fail(EFG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return efg::fail(EFG_ERR_ARG, "device ordinal beyond the scratch table");
+  std::lock_guard<std::mutex> g(g_mu);
+  if (!g_dev_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_bf_scratch);
+    if (e != cudaSuccess || !p)
+      return efg::fail(EFG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_dev_ptr[dev] = static_cast<uint64_t*>(p);
+  }
+  *out = g_dev_ptr[dev];
+  return EFG_OK;
+}
+
+}  // namespace
+
+extern "C" int efg_brute_force_knn_noalloc(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride,
+                                           const float* d_q, uint64_t nq, uint64_t q_stride, uint32_t k,
+                                           int exclude_self, uint64_t first_row, int32_t* d_ids, float* d_dists,
+                                           void* stream) {
+  using efg::fail;
+  if (!d_base || (!d_q && nq) || (!d_ids && nq)) return fail(EFG_ERR_ARG, "null argument");
+  if (k == 0 || k > 256) return fail(EFG_ERR_ARG, "k must be in [1, 256]");
+  if ((uint64_t)k + (exclude_self ? 1 : 0) > n) return fail(EFG_ERR_ARG, "k larger than the base");
+  if (row_stride < dim || q_stride < dim || (row_stride % 4) || (q_stride % 4) || (((uintptr_t)d_base) & 15) ||
+      (((uintptr_t)d_q) & 15))
+    return fail(EFG_ERR_ARG, "rows must be 16-byte aligned: strides a multiple of 4 floats");
+  uint64_t* scratch = nullptr;
+  int rc = scratch_address(&scratch);
+  if (rc != EFG_OK) return rc;
+  return efg::brute_force_knn_in(d_base, n, dim, (uint32_t)row_stride, d_q, nq, (uint32_t)q_stride, k, exclude_self,
+                                 first_row, d_ids, d_dists, scratch, kScratchEntries, (cudaStream_t)stream);
+}

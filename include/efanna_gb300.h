@@ -149,6 +149,20 @@ int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t 
                         uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
                         int32_t* d_ids, float* d_dists, void* stream);
 
+/* efg_brute_force_knn without any device allocation, for callers that must not have a library
+ * allocate GPU memory during the call (their device memory is owned by another allocator, or the
+ * call sits in a loop that cannot afford an allocation).  No counterpart in the reference.
+ * Same arguments and results as efg_brute_force_knn.  Its scratch is a fixed array compiled into
+ * the library (EFG_BF_NOALLOC_SCRATCH_ENTRIES 8-byte entries = 16 MiB, held on every GPU that loads
+ * the library until exit); calls needing more than nq * (k + 16) <= that many entries return
+ * EFG_ERR_ARG.  The first call on a device looks up the scratch address (cudaGetSymbolAddress),
+ * so make it before any stream capture.  All calls share the scratch: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+#define EFG_BF_NOALLOC_SCRATCH_ENTRIES (1ull << 21)
+int efg_brute_force_knn_noalloc(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride,
+                                const float* d_q, uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self,
+                                uint64_t first_row, int32_t* d_ids, float* d_dists, void* stream);
+
 /* NN-descent state on the host, for state-level parity checks (one layout with the oracle):
  * pool arrays are n*(L+1), list arrays n*cap.  efg_nnd_init runs the leaf-merge initial
  * graph on the index's trees (initGraph, kdtreeub_index.hpp:1367-1424); efg_nnd_iterate runs

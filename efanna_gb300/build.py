@@ -37,7 +37,7 @@ def _flags():
 def _compile(src: str) -> str:
     obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
+    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".inc"))]
     deps.append(os.path.join(ROOT, "include", "efanna_gb300.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj

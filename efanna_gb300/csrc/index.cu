@@ -300,6 +300,7 @@ void efg_index_destroy(efg_index* idx) {
   idx->out_buf.release();
   idx->eval_counter.release();
   idx->ht_scratch.release();
+  idx->ovf_list.release();
   if (idx->d_base) cudaFree(idx->d_base);
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;

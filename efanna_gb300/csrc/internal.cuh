@@ -55,9 +55,10 @@ struct Forest {
   // SoA build-side arrays (kept after a device build; used by the leaf merge)
   DevBuf<int32_t> n_left, n_right, n_level, n_tree;
   DevBuf<uint32_t> n_start, n_end;
+  DevBuf<int32_t> nleaf;                // leaves in each node's subtree (search descent ranks)
   bool has_soa = false;
   void release() {
-    nodes.release(); d_roots.release(); leaves.release();
+    nodes.release(); d_roots.release(); leaves.release(); nleaf.release();
     n_left.release(); n_right.release(); n_level.release(); n_tree.release(); n_start.release(); n_end.release();
     ntrees = 0; nnodes = 0; roots.clear(); has_soa = false;
   }
@@ -97,6 +98,7 @@ struct efg_index {
   efg::DevBuf<int32_t> out_buf;
   efg::DevBuf<unsigned long long> eval_counter;
   efg::DevBuf<uint32_t> ht_scratch;  // per-CTA visited sets when they do not fit in shared memory
+  efg::DevBuf<uint32_t> ovf_list;    // queries handed from the first search pass to the overflow pass
 };
 
 namespace efg {

@@ -291,6 +291,14 @@ __global__ void to_dnodes_kernel(NodeArrays na, uint32_t nnodes, DNode* __restri
   out[v] = d;
 }
 
+// Leaves per subtree for the nodes [lo, hi) of one level; deeper levels are already done.
+__global__ void leaf_count_kernel(const int32_t* __restrict__ left, const int32_t* __restrict__ right, int32_t lo,
+                                  int32_t hi, int32_t* __restrict__ nleaf) {
+  int32_t v = lo + (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (v >= hi) return;
+  nleaf[v] = left[v] < 0 ? 1 : nleaf[left[v]] + nleaf[right[v]];
+}
+
 static unsigned grid_for(uint64_t total, int threads) {
   return (unsigned)std::min<uint64_t>((total + threads - 1) / threads, 152ull * 32);
 }
@@ -353,6 +361,7 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
 
   uint32_t nactive = ntrees;
   int32_t nnodes = (int32_t)ntrees;
+  std::vector<std::pair<int32_t, int32_t>> level_ranges{{0, (int32_t)ntrees}};
   bool phaseA = true;
   int32_t level = 0;
   uint32_t* cur = F.leaves.p;
@@ -388,6 +397,7 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
     uint32_t nnext = 0;
     EFG_CUDA(cudaMemcpyAsync(&nnext, next_pos.p + 2ull * nactive, 4, cudaMemcpyDeviceToHost, s));
     EFG_CUDA(cudaStreamSynchronize(s));
+    level_ranges.push_back({nnodes, nnodes + 2 * (int32_t)nsplit});
     nnodes += 2 * (int32_t)nsplit;
     nactive = nnext;
     ++level;
@@ -398,6 +408,11 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
     EFG_CUDA(cudaMemcpyAsync(F.leaves.p, cur, total * 4, cudaMemcpyDeviceToDevice, s));
   EFG_TRY(F.nodes.reserve(nnodes));
   to_dnodes_kernel<<<(nnodes + 255) / 256, 256, 0, s>>>(na, (uint32_t)nnodes, F.nodes.p);
+  EFG_TRY(F.nleaf.reserve(nnodes));
+  for (size_t l = level_ranges.size(); l-- > 0;) {
+    int32_t lo = level_ranges[l].first, hi = level_ranges[l].second;
+    if (hi > lo) leaf_count_kernel<<<(hi - lo + 255) / 256, 256, 0, s>>>(na.left, na.right, lo, hi, F.nleaf.p);
+  }
   EFG_CUDA(cudaGetLastError());
   // keep dim/val in the DNode array; the SoA start/end/tree/level/left/right stay for the merge
   EFG_TRY(F.d_roots.reserve(ntrees));
@@ -462,6 +477,25 @@ int upload_forest(efg_index* idx, const std::vector<HNode>& nodes, const std::ve
     }
   }
   size_t m = nodes.size();
+  std::vector<int32_t> nl(m, 0);
+  for (uint32_t t = 0; t < ntrees; ++t) {  // post-order leaf counts
+    std::vector<std::pair<int32_t, bool>> stack{{roots[t], false}};
+    while (!stack.empty()) {
+      auto [v, done] = stack.back();
+      stack.pop_back();
+      if (l[v] < 0) {
+        nl[v] = 1;
+      } else if (done) {
+        nl[v] = nl[l[v]] + nl[r[v]];
+      } else {
+        stack.push_back({v, true});
+        stack.push_back({l[v], false});
+        stack.push_back({r[v], false});
+      }
+    }
+  }
+  EFG_TRY(F.nleaf.reserve(m));
+  EFG_CUDA(cudaMemcpy(F.nleaf.p, nl.data(), m * 4, cudaMemcpyHostToDevice));
   EFG_TRY(F.nodes.reserve(m));
   EFG_TRY(F.d_roots.reserve(ntrees));
   EFG_TRY(F.leaves.reserve(leaves.size()));

@@ -1,6 +1,13 @@
-"""Summaries of Nsight Compute CSV output (per-kernel launch counts, total time and share)."""
+"""Profiling helpers.
+
+    python -m efanna_gb300.profiling table <ncu.csv>        per-kernel launch counts, time, share
+    python -m efanna_gb300.profiling search [--n N] [--nq Q] [--point E P X] [--trees T]
+        builds a graph on the seeded mixture and runs one batched search: the small case used
+        for Nsight Compute captures of nnexp_kernel (N=400k keeps the base above the L2 size).
+"""
 from __future__ import annotations
 
+import argparse
 import collections
 import csv
 import sys
@@ -31,5 +38,45 @@ def launch_table(path: str, metric: str = "gpu__time_duration.sum"):
     return "\n".join(out)
 
 
+def search_case(n: int, nq: int, point, trees: int, extra=None) -> None:
+    import time
+
+    import efanna_gb300 as E
+    from efanna_gb300 import datasets
+    x = datasets.mixture_u8(n, 128, seed=0)
+    q = datasets.mixture_u8(nq, 128, seed=0, queries=True)
+    idx = E.Index(x, E.IndexParams(trees=8, merge_level=8, epochs=8, check=25, L=30, K=10, S=10))
+    idx.build_index()
+    idx.build_trees(trees)
+    pts = [point] + list(extra or [])
+    for pt in pts:
+        idx.set_search_params(pt[0], pt[1], pt[2], trees)
+        idx.knn_search(10, q)
+        t0 = time.perf_counter()
+        idx.knn_search(10, q)
+        s = idx.search_stats()
+        print("search %d/%d/%d, %d queries: %.3f ms kernel, %.1f evals/query, %d overflow, wall %.3f s" %
+              (pt[0], pt[1], pt[2], nq, s.device_ms, s.distance_evals / nq, s.overflow_queries,
+               time.perf_counter() - t0))
+
+
 if __name__ == "__main__":
-    print(launch_table(sys.argv[1]))
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd")
+    t = sub.add_parser("table")
+    t.add_argument("csv")
+    s = sub.add_parser("search")
+    s.add_argument("--n", type=int, default=400000)
+    s.add_argument("--nq", type=int, default=2000)
+    s.add_argument("--point", type=int, nargs=3, default=[8, 6000, 600])
+    s.add_argument("--trees", type=int, default=16)
+    s.add_argument("--also", type=int, nargs=3, action="append", default=[],
+                   help="further epochs/pool/extend points to time after --point")
+    a = ap.parse_args()
+    if a.cmd == "table":
+        print(launch_table(a.csv))
+    elif a.cmd == "search":
+        search_case(a.n, a.nq, a.point, a.trees, a.also)
+    else:
+        ap.print_help()
+        sys.exit(1)

@@ -71,6 +71,7 @@ typedef struct efg_search_stats {
   uint64_t distance_evals;  /* query-to-base distances computed by the last search call         */
   uint64_t queries;
   uint64_t expanded_nodes;  /* graph rows read by the expansion epochs of the last search call  */
+  uint64_t overflow_queries; /* queries whose visited set outgrew shared memory (second pass)   */
 } efg_search_stats;
 
 typedef struct efg_index efg_index;

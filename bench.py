@@ -169,105 +169,122 @@ def run_gpu(args):
         idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
         idx.knn_search_device(10, Q.data_ptr(), nq, 128, out.data_ptr(), stream.cuda_stream)
 
-    # operating point: first ladder entry reaching the target recall
-    ladder = []
-    point = None
-    for pt in LADDER:
-        try:
-            search_once(pt)
-            torch.cuda.synchronize()
-        except E.EfannaError as e:
-            log("skip", pt, e)
-            continue
-        rc = recall(out.cpu().numpy(), gt)
-        ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4)})
-        if rc >= TARGET:
-            point = pt
-            break
-    if point is None:
-        point = LADDER[-1]
-    res_cfg = None
-    search_once(CONFIG_POINT)
-    torch.cuda.synchronize()
-    res_cfg = recall(out.cpu().numpy(), gt)
-    # evals / expansions at the operating point (host API fills the stats)
-    idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
-    res_host = idx.knn_search(10, q)
-    st = idx.search_stats()
-    op_recall = recall(res_host, gt)
-    evals_q = st.distance_evals / nq
-    exp_q = st.expanded_nodes / nq
-    # algorithmic bytes per query: candidate rows + graph rows of expanded nodes + leaf ids + query
-    bytes_q = evals_q * 128 * 4 + exp_q * GRAPH["K"] * 4 + point[1] * 4 + 128 * 4
+    def measure(precision):
+        """Operating point, device-timed QPS, e2e QPS and roofline inputs for one search precision."""
+        idx.set_search_precision(precision)
+        ladder, point = [], None
+        for pt in LADDER:  # first ladder entry reaching the target recall
+            try:
+                search_once(pt)
+                torch.cuda.synchronize()
+            except E.EfannaError as e:
+                log("skip", pt, e)
+                continue
+            rc = recall(out.cpu().numpy(), gt)
+            ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4)})
+            if rc >= TARGET:
+                point = pt
+                break
+        if point is None:
+            point = LADDER[-1]
+        search_once(CONFIG_POINT)
+        torch.cuda.synchronize()
+        res_cfg = recall(out.cpu().numpy(), gt)
+        # evals / expansions / launches at the operating point (the host API fills the stats)
+        idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
+        res_host = idx.knn_search(10, q)
+        st = idx.search_stats()
+        evals_q = st.distance_evals / nq
+        exp_q = st.expanded_nodes / nq
+        row_bytes = 128 * (2 if precision == "bf16" else 4)
+        # algorithmic bytes per query: screened rows + graph rows of expanded nodes + leaf ids + query
+        # (+ the FP32 rows re-ranked after BF16 screening)
+        bytes_q = evals_q * row_bytes + exp_q * GRAPH["K"] * 4 + point[1] * 4 + 128 * 4 + st.reranked * 128 * 4
+        for _ in range(args.warmup):
+            search_once(point)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        clocks = ClockSampler()
+        clocks.start()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            search_once(point)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        ck = clocks.stop()
+        ms = ev0.elapsed_time(ev1)
+        ms_t = torch.tensor([ms], device=dev)
+        if ws > 1:
+            torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(ms_t.item())
+        # end to end through the host API (queries host->device, ids device->host inside the region)
+        for _ in range(max(1, args.warmup // 2)):
+            idx.knn_search(10, q)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            idx.knn_search(10, q)
+        e2e_s = time.perf_counter() - t0
+        return {"precision": precision, "point": point, "ladder": ladder, "config_recall": res_cfg,
+                "recall": recall(res_host, gt), "ms": ms, "per_step_ms": ms / args.steps,
+                "value": ws * nq * args.steps / (ms / 1e3), "e2e": ws * nq * args.steps / e2e_s,
+                "evals_q": evals_q, "exp_q": exp_q, "bytes_q": bytes_q, "launches": int(st.kernel_launches),
+                "overflow": int(st.overflow_queries), "reranked": int(st.reranked), "clocks": ck}
 
-    # the timed region
-    for _ in range(args.warmup):
-        search_once(point)
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler()
-    clocks.start()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        search_once(point)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    ck = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    ms_t = torch.tensor([ms], device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    per_step_ms = ms / args.steps
-    value = ws * nq * args.steps / (ms / 1e3)
-    launch_ms = per_step_ms  # one nnexp launch per step, timed on its own stream
-
-    # end to end through the host API
-    for _ in range(max(1, args.warmup // 2)):
-        idx.knn_search(10, q)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        idx.knn_search(10, q)
-    e2e_s = time.perf_counter() - t0
-    e2e = ws * nq * args.steps / e2e_s
-
+    runs = {p: measure(p) for p in ("fp32", "bf16")}
+    idx.set_search_precision("fp32")
     hbm, peak_kind = peaks()
-    achieved = bytes_q * nq / (launch_ms / 1e3) / 1e9
+
+    def roofline(r):
+        # one search launch per step (plus the overflow launch when queries overflow), timed on its stream
+        achieved = r["bytes_q"] * nq / (r["per_step_ms"] / 1e3) / 1e9
+        return {"bound": "hbm", "kernel": "nnexp_kernel", "achieved": round(achieved, 1), "peak": hbm,
+                "peak_kind": peak_kind + " (burst)", "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                "algorithmic_bytes_per_query": round(r["bytes_q"], 1),
+                "distance_evals_per_query": round(r["evals_q"], 1), "expanded_per_query": round(r["exp_q"], 1),
+                "traffic": None}
+
+    def point_of(r):
+        pt = r["point"]
+        return {"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(r["recall"], 4)}
+
+    f32, b16 = runs["fp32"], runs["bf16"]
     line = {
-        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(per_step_ms, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded integer-valued Gaussian mixture)",
+        "metric": METRIC, "value": round(f32["value"], 1), "unit": "queries/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(f32["per_step_ms"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded integer-valued Gaussian mixture)",
         "config": {"workload": "1M x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), "
                                "16 search trees, 10k queries, k=10",
                    "n": args.n, "dim": 128, "queries": nq, "k": 10, "search_trees": SEARCH_TREES,
-                   "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2],
-                                       "recall@10": round(op_recall, 4)},
+                   "operating_point": point_of(f32),
                    "config_point": {"epochs": CONFIG_POINT[0], "pool": CONFIG_POINT[1], "extend": CONFIG_POINT[2],
-                                    "recall@10": round(res_cfg, 4)},
-                   "ladder": ladder, "l2": "inputs larger than L2 (512 MB base), no flush",
+                                    "recall@10": round(f32["config_recall"], 4)},
+                   "ladder": f32["ladder"], "l2": "inputs larger than L2 (512 MB base), no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "build": {"graph_build_s": round(min(build_s), 4), "graph_build_s_runs": [round(b, 4) for b in build_s],
                   "trees_ms": round(bst.trees_ms, 2), "init_ms": round(bst.init_ms, 2),
                   "refine_ms": round(bst.refine_ms, 2), "join_pairs": int(bst.join_pairs),
                   "graph_recall@10": round(graph_recall, 4), "search_trees16_s": round(trees_s, 4)},
-        "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+        "e2e": {"value": round(f32["e2e"], 1), "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(nq * 10 * 4)},
-        "roofline": {"bound": "hbm", "kernel": "nnexp_kernel", "achieved": round(achieved, 1), "peak": hbm,
-                     "peak_kind": peak_kind + " (burst)", "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "algorithmic_bytes_per_query": round(bytes_q, 1), "distance_evals_per_query": round(evals_q, 1),
-                     "expanded_per_query": round(exp_q, 1),
-                     "traffic": None},
-        "gpu_launches": args.steps,
-        "clocks": ck,
+        "roofline": roofline(f32),
+        "bf16": {"value": round(b16["value"], 1), "unit": "queries/s", "ms_per_step": round(b16["per_step_ms"], 4),
+                 "e2e": round(b16["e2e"], 1), "operating_point": point_of(b16), "ladder": b16["ladder"],
+                 "config_point_recall@10": round(b16["config_recall"], 4), "reranked_per_query": b16["reranked"],
+                 "roofline": roofline(b16), "gpu_launches": b16["launches"] * args.steps,
+                 "clocks": b16["clocks"],
+                 "form": "BF16 copy of the base screens the walk, the best max(2k, k+32) re-ranked in FP32"},
+        "gpu_launches": f32["launches"] * args.steps,
+        "clocks": f32["clocks"],
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(x, q, gt, point, idx, args)
+        line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     idx.close()

@@ -44,7 +44,8 @@ class BuildStats(C.Structure):
 
 class SearchStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("distance_evals", C.c_uint64), ("queries", C.c_uint64),
-                ("expanded_nodes", C.c_uint64), ("overflow_queries", C.c_uint64)]
+                ("expanded_nodes", C.c_uint64), ("overflow_queries", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("reranked", C.c_uint64)]
 
 
 class HostState(C.Structure):
@@ -102,6 +103,7 @@ def lib():
         "efg_build_graph": (i32, [vp]),
         "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
         "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
+        "efg_set_search_precision": (i32, [vp, i32]),
         "efg_knn_search": (i32, [vp, f32p, u64, u32, u64, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_device": (i32, [vp, vp, u64, u64, u32, vp, vp]),
         "efg_get_search_stats": (i32, [vp, C.POINTER(SearchStats)]),
@@ -196,6 +198,13 @@ class Index:
                           search_lv: int = -1, search_method: int = 0) -> None:
         _check(lib().efg_set_search_params(self._h, epochs, init_num, extend_to, search_trees, search_lv,
                                            search_method))
+
+    def set_search_precision(self, precision: str) -> None:
+        """'fp32' (the reference's arithmetic) or 'bf16' (BF16 screening, FP32 re-rank)."""
+        code = {"fp32": 0, "bf16": 1}.get(precision)
+        if code is None:
+            raise ValueError("precision must be 'fp32' or 'bf16'")
+        _check(lib().efg_set_search_precision(self._h, code))
 
     def knn_search(self, k: int, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, dtype=np.float32)

@@ -301,6 +301,7 @@ void efg_index_destroy(efg_index* idx) {
   idx->eval_counter.release();
   idx->ht_scratch.release();
   idx->ovf_list.release();
+  idx->base16.release();
   if (idx->d_base) cudaFree(idx->d_base);
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;
@@ -346,6 +347,15 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
   sp.search_lv = search_lv;
   sp.search_trees = search_trees;
   sp.method = search_method;
+  return EFG_OK;
+}
+
+int efg_set_search_precision(efg_index* idx, int precision) {
+  if (!idx) return fail(EFG_ERR_ARG, "null index");
+  if (precision != EFG_PRECISION_FP32 && precision != EFG_PRECISION_BF16)
+    return fail(EFG_ERR_ARG, "precision must be EFG_PRECISION_FP32 or EFG_PRECISION_BF16");
+  if (precision == EFG_PRECISION_BF16 && !idx->base16.p) EFG_TRY(make_base16(idx));
+  idx->precision = precision;
   return EFG_OK;
 }
 

@@ -99,6 +99,10 @@ struct efg_index {
   efg::DevBuf<unsigned long long> eval_counter;
   efg::DevBuf<uint32_t> ht_scratch;  // per-CTA visited sets when they do not fit in shared memory
   efg::DevBuf<uint32_t> ovf_list;    // queries handed from the first search pass to the overflow pass
+  // search precision: 0 = FP32 rows, 1 = BF16 screening copy (base16, ld16 values per row) + FP32 re-rank
+  int precision = 0;
+  efg::DevBuf<uint16_t> base16;
+  uint32_t ld16 = 0;
 };
 
 namespace efg {
@@ -121,6 +125,8 @@ int download_forest(efg_index* idx, std::vector<HNode>& nodes, std::vector<uint3
 // search.cu
 int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                   cudaStream_t s, bool count_evals);
+// Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
+int make_base16(efg_index* idx);
 
 // nndescent.cu
 struct NNDState;

@@ -28,6 +28,8 @@
 // launch answers the listed queries with a worst-case-sized table in global memory.
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "internal.cuh"
 
 namespace efg {
@@ -55,6 +57,10 @@ struct SearchCfg {
   uint32_t o_ids, o_ht, o_u;
   uint32_t o_lstart, o_lend, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
   uint32_t o_res, o_tmp, o_newk, o_surv;                // select phase (absolute)
+  uint32_t q4;          // staged query length in float4 (covers both row layouts)
+  // BF16 screening: rows ld16 values apart, cpr16 16-byte chunks per row, 2^gshift16 lanes per
+  // row in the gather; the first `rerank` results are re-scored in FP32 before the k are emitted
+  uint32_t bf16, ld16, cpr16, gshift16, rerank;
   uint64_t seed;
 };
 
@@ -137,6 +143,29 @@ static constexpr int S_WARPS = S_THREADS / 32;
 #include "search_kernel.inc"
 }  // namespace s512
 
+__global__ void to_bf16_kernel(const float* __restrict__ base, uint64_t n, uint32_t dim, uint32_t ld,
+                               uint16_t* __restrict__ out, uint32_t ld16) {
+  uint64_t total = n * ld16;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t r = i / ld16;
+    uint32_t c = (uint32_t)(i - r * ld16);
+    float v = c < dim ? base[r * ld + c] : 0.f;
+    out[i] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  }
+}
+
+int make_base16(efg_index* idx) {
+  idx->ld16 = (uint32_t)round_up(idx->dim, 8);
+  EFG_TRY(idx->base16.reserve(idx->n * idx->ld16));
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  to_bf16_kernel<<<sms * 8, 256, 0, idx->stream>>>(idx->d_base, idx->n, idx->dim, idx->ld, idx->base16.p, idx->ld16);
+  EFG_CUDA(cudaGetLastError());
+  EFG_CUDA(cudaStreamSynchronize(idx->stream));
+  return EFG_OK;
+}
+
 int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                   cudaStream_t s, bool count_evals) {
   const SearchParams& sp = idx->sp;
@@ -160,6 +189,17 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
   cfg.k = k;
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
+  if (idx->precision == EFG_PRECISION_BF16) {
+    if (!idx->base16.p) EFG_TRY(make_base16(idx));
+    cfg.bf16 = 1;
+    cfg.ld16 = idx->ld16;
+    cfg.cpr16 = idx->ld16 / 8;
+    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr16), 32);
+    while ((1u << cfg.gshift16) < g) ++cfg.gshift16;
+    cfg.rerank = std::min<uint32_t>(std::min<uint32_t>(std::max(2 * k, k + 32), cfg.result_size),
+                                    (uint32_t)SEL_CHUNK);
+    if (k > cfg.rerank) return fail(EFG_ERR_ARG, "k above 1024 is not supported with BF16 screening");
+  }
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
   uint32_t maxdeg = idx->graph.fixed_k;
@@ -226,12 +266,13 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
       idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
       idx->graph.ids.p, d_q, nq, qld, c1, d_out, idx->eval_counter.p, idx->ht_scratch.p, nullptr,
-      two_pass ? idx->ovf_list.p : nullptr);
+      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p);
   cudaError_t le = cudaGetLastError();
   if (le == cudaSuccess && two_pass) {
     kernel<<<(unsigned)grid2, threads, smem2, s>>>(
         idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
-        idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr);
+        idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr,
+        idx->base16.p);
     le = cudaGetLastError();
   }
   cudaEventRecord(e1, s);
@@ -253,6 +294,8 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
     idx->sstats.queries = nq;
     idx->sstats.expanded_nodes = h[2];
     idx->sstats.overflow_queries = novf;
+    idx->sstats.kernel_launches = two_pass ? 2 : 1;
+    idx->sstats.reranked = cfg.bf16 ? std::min<uint32_t>(cfg.rerank, cfg.result_size) : 0;
     if (h[1] & SERR_FRONTIER) return fail(EFG_ERR_DEVICE_LIMIT, "tree descent frontier overflow");
     if (h[1] & SERR_HASH) return fail(EFG_ERR_DEVICE_LIMIT, "candidate buffer overflow");
   }

@@ -72,6 +72,8 @@ typedef struct efg_search_stats {
   uint64_t queries;
   uint64_t expanded_nodes;  /* graph rows read by the expansion epochs of the last search call  */
   uint64_t overflow_queries; /* queries whose visited set outgrew shared memory (second pass)   */
+  uint64_t kernel_launches;  /* search kernels launched by the last search call (1 or 2)         */
+  uint64_t reranked;         /* FP32 re-rank distances per query under BF16 screening (0 in FP32) */
 } efg_search_stats;
 
 typedef struct efg_index efg_index;
@@ -101,6 +103,16 @@ int efg_get_build_stats(const efg_index* idx, efg_build_stats* out);
  * init_num).  search_method 0 = nnexp (kdtreeub_index.hpp:363-494), 1 = kgraph (:496-654). */
 int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_to, int search_trees,
                           int search_lv, int search_method);
+
+/* Search precision (no reference counterpart; the reference computes in FP32 only).
+ * EFG_PRECISION_FP32: every distance from the FP32 rows, results as the reference's.
+ * EFG_PRECISION_BF16: the search walks the graph with distances from a BF16 copy of the base
+ * (half the bytes per row; made on the first call that selects it and kept with the index), then
+ * re-scores its best max(2k, k + 32) candidates (at most 1024) from the FP32 rows and emits the k
+ * best of those.  Ids can differ from the FP32 search where BF16 rounding reorders candidates. */
+#define EFG_PRECISION_FP32 0
+#define EFG_PRECISION_BF16 1
+int efg_set_search_precision(efg_index* idx, int precision);
 
 /* FIndex::knnSearch — efanna.hpp:32-34, base_index.hpp:311-313.  Host queries in, host ids out
  * (nq*k int32).  The ids are also kept for efg_save_results. */

@@ -2,8 +2,10 @@
 
     python -m efanna_gb300.profiling table <ncu.csv>        per-kernel launch counts, time, share
     python -m efanna_gb300.profiling search [--n N] [--nq Q] [--point E P X] [--trees T]
-        builds a graph on the seeded mixture and runs one batched search: the small case used
-        for Nsight Compute captures of nnexp_kernel (N=400k keeps the base above the L2 size).
+                                            [--precision fp32|bf16 ...] [--repeat R]
+        builds a graph on the seeded mixture and runs batched searches (R per precision and
+        point): the small case used for Nsight Compute captures of nnexp_kernel (N=400k keeps
+        the base above the L2 size).
 """
 from __future__ import annotations
 
@@ -38,7 +40,7 @@ def launch_table(path: str, metric: str = "gpu__time_duration.sum"):
     return "\n".join(out)
 
 
-def search_case(n: int, nq: int, point, trees: int, extra=None) -> None:
+def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2) -> None:
     import time
 
     import efanna_gb300 as E
@@ -49,15 +51,18 @@ def search_case(n: int, nq: int, point, trees: int, extra=None) -> None:
     idx.build_index()
     idx.build_trees(trees)
     pts = [point] + list(extra or [])
-    for pt in pts:
-        idx.set_search_params(pt[0], pt[1], pt[2], trees)
-        idx.knn_search(10, q)
-        t0 = time.perf_counter()
-        idx.knn_search(10, q)
-        s = idx.search_stats()
-        print("search %d/%d/%d, %d queries: %.3f ms kernel, %.1f evals/query, %d overflow, wall %.3f s" %
-              (pt[0], pt[1], pt[2], nq, s.device_ms, s.distance_evals / nq, s.overflow_queries,
-               time.perf_counter() - t0))
+    for prec in precisions:
+        idx.set_search_precision(prec)
+        for pt in pts:
+            idx.set_search_params(pt[0], pt[1], pt[2], trees)
+            for _ in range(repeat):
+                t0 = time.perf_counter()
+                idx.knn_search(10, q)
+                s = idx.search_stats()
+                print("search %s %d/%d/%d, %d queries: %.3f ms kernel (%d launches), %.1f evals/query, "
+                      "%.1f expanded/query, %d overflow, wall %.3f s" %
+                      (prec, pt[0], pt[1], pt[2], nq, s.device_ms, s.kernel_launches, s.distance_evals / nq,
+                       s.expanded_nodes / nq, s.overflow_queries, time.perf_counter() - t0))
 
 
 if __name__ == "__main__":
@@ -72,11 +77,13 @@ if __name__ == "__main__":
     s.add_argument("--trees", type=int, default=16)
     s.add_argument("--also", type=int, nargs=3, action="append", default=[],
                    help="further epochs/pool/extend points to time after --point")
+    s.add_argument("--precision", nargs="+", default=["fp32"], choices=["fp32", "bf16"])
+    s.add_argument("--repeat", type=int, default=2)
     a = ap.parse_args()
     if a.cmd == "table":
         print(launch_table(a.csv))
     elif a.cmd == "search":
-        search_case(a.n, a.nq, a.point, a.trees, a.also)
+        search_case(a.n, a.nq, a.point, a.trees, a.also, a.precision, a.repeat)
     else:
         ap.print_help()
         sys.exit(1)

@@ -1255,15 +1255,16 @@ struct SearchArgs {
   uint32_t k;
 };
 
-static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, const uint32_t* gids, const float* q,
-                       uint64_t qi, const SearchArgs& a, int mode, uint64_t seed, int32_t* out, uint64_t* nd) {
+// Pool seeding shared by both search methods (kdtreeub_index.hpp:380-418 and :519-548): leaves of
+// the near-first DFS of every tree, leaf rank outer and tree inner, first occurrences until
+// init_num; short pools are topped up with random ids (std::rand() in sequential mode, the
+// per-query counter hash in canonical mode).  tbflag marks the pool's ids.
+static std::vector<int> fill_pool(const Data& X, const Forest& F, const float* q, uint64_t qi, unsigned T,
+                                  unsigned lsize, unsigned init_num, int mode, uint64_t seed,
+                                  std::vector<uint8_t>& tbflag) {
   size_t N = X.n;
-  std::vector<uint8_t> tbflag(N, 0), newflag(N, 1);
-  unsigned T = (unsigned)a.trees;
-  unsigned lsize = a.init_num * 2 / (5 * T) + 1;
   std::vector<std::vector<int32_t>> cand(T);
   for (unsigned t = 0; t < T; ++t) search_node_list(F, t, F.roots[t], q, lsize, cand[t]);
-  unsigned init_num = (unsigned)a.init_num;
   std::vector<int> pool(init_num);
   unsigned pcount = 0;
   for (unsigned ni = 0; ni < lsize; ni++) {
@@ -1297,6 +1298,16 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
       pool[pcount++] = (int)id;
     }
   }
+  return pool;
+}
+
+static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, const uint32_t* gids, const float* q,
+                       uint64_t qi, const SearchArgs& a, int mode, uint64_t seed, int32_t* out, uint64_t* nd) {
+  size_t N = X.n;
+  std::vector<uint8_t> tbflag(N, 0), newflag(N, 1);
+  unsigned T = (unsigned)a.trees;
+  unsigned lsize = a.init_num * 2 / (5 * T) + 1;
+  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, tbflag);
   unsigned resultSize = (unsigned)a.extend_to;
   if (a.k > resultSize) resultSize = a.k;
   std::vector<std::pair<float, size_t>> result;
@@ -1329,6 +1340,132 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
     for (unsigned j = 0; j < resultSize; j++) pool.push_back((int)result[j].second);
   }
   for (uint32_t i = 0; i < a.k; i++) out[i] = pool[i];
+  if (nd) *nd = evals;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Search: getNeighbors_kgraph (kdtreeub_index.hpp:496-654).
+// ----------------------------------------------------------------------------------------------
+// Point (base_index.hpp:24-34): ordered by dist only.  `id == UINT32_MAX` stands for the
+// reference's default-constructed (uninitialised) Point.
+struct KPoint {
+  uint32_t id;
+  float dist;
+  bool flag;
+  bool operator<(const KPoint& o) const { return dist < o.dist; }
+};
+static inline bool canon_less(const KPoint& a, const KPoint& b) {
+  return a.dist < b.dist || (a.dist == b.dist && a.id < b.id);
+}
+
+// InsertIntoKnn (base_index.hpp:37-62): insert after the entries of equal distance, reject a
+// duplicate id among them (returns K + 1); writes addr[K] (the slot past the live list).
+static unsigned insert_knn_seq(KPoint* addr, unsigned K, KPoint nn) {
+  unsigned i = K;
+  while (i > 0) {
+    if (addr[i - 1].dist <= nn.dist) break;
+    --i;
+  }
+  unsigned l = i;
+  while (l > 0) {
+    if (addr[l - 1].dist < nn.dist) break;
+    if (addr[l - 1].id == nn.id) return K + 1;
+    --l;
+  }
+  for (unsigned j = K; j > i; --j) addr[j] = addr[j - 1];
+  addr[i] = nn;
+  return i;
+}
+// Canonical counterpart: the position by (dist, id); ids are unique here, so no duplicate test.
+static unsigned insert_knn_canon(KPoint* addr, unsigned K, KPoint nn) {
+  unsigned i = K;
+  while (i > 0 && canon_less(nn, addr[i - 1])) --i;
+  for (unsigned j = K; j > i; --j) addr[j] = addr[j - 1];
+  addr[i] = nn;
+  return i;
+}
+
+// One query of getNeighbors_kgraph.  init_num is the pool size in effect for this call (the
+// caller applies the reference's enlargement to epochs * extend_to) and lsize the per-tree leaf
+// count computed from the pool size before that enlargement (:507, :510-514).
+static void search_one_kgraph(const Data& X, const Forest& F, const uint64_t* gptr, const uint32_t* gids,
+                              const float* q, uint64_t qi, const SearchArgs& a, unsigned lsize, bool sorted,
+                              int mode, uint64_t seed, int32_t* out, uint64_t* nd) {
+  size_t N = X.n;
+  const unsigned T = (unsigned)a.trees, E = (unsigned)a.extend_to, epochs = (unsigned)a.epochs;
+  const unsigned searchK = a.k, pool_size = epochs * E;
+  std::vector<uint8_t> flags(N, 0);
+  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, flags);
+  std::vector<std::pair<float, size_t>> result;  // :551-566, in pool order
+  for (unsigned j = 0; j < pool.size(); ++j) result.push_back({X.distq(q, X.row(pool[j])), (size_t)pool[j]});
+  uint64_t evals = pool.size();
+  if (sorted) {  // :567-570
+    std::partial_sort(result.begin(), result.begin() + pool_size, result.end());
+    result.resize(pool_size);
+  }
+  std::fill(flags.begin(), flags.end(), 0);  // flags.reset() (:572)
+  const bool seq = mode == MODE_SEQ;
+  auto insert = seq ? insert_knn_seq : insert_knn_canon;
+  std::vector<KPoint> knn(searchK + E + 1);
+  std::vector<KPoint> results;
+  for (unsigned iter = 0; iter < epochs; ++iter) {
+    unsigned L = 0;
+    for (unsigned j = 0; j < E; j++) {  // :577-585
+      const auto& r = result[iter * E + j];
+      if (!flags[r.second]) {
+        flags[r.second] = 1;
+        knn[L].id = (uint32_t)r.second;
+        knn[L].dist = r.first;
+        knn[L].flag = true;
+        L++;
+      }
+    }
+    if (seq) std::sort(knn.begin(), knn.begin() + L);  // `if(~bSorted)` is always true (:587-589)
+    else std::sort(knn.begin(), knn.begin() + L, canon_less);
+    unsigned k = 0;
+    while (k < L) {  // :591-631
+      unsigned nk = L;
+      if (knn[k].flag) {
+        knn[k].flag = false;
+        unsigned n = knn[k].id;
+        unsigned maxM = E;
+        unsigned deg = (unsigned)(gptr[n + 1] - gptr[n]);
+        if (maxM > deg) maxM = deg;
+        for (unsigned m = 0; m < maxM; ++m) {
+          unsigned id = gids[gptr[n] + m];
+          if (flags[id]) continue;
+          flags[id] = 1;
+          KPoint nn{id, X.distq(q, X.row(id)), true};
+          ++evals;
+          unsigned r = insert(&knn[0], L, nn);
+          if (L + 1 < knn.size()) ++L;
+          if (r < nk) nk = r;
+        }
+      }
+      if (nk <= k) k = nk;
+      else ++k;
+    }
+    if (L > searchK) L = searchK;
+    if (results.empty()) {  // :634-646
+      results.resize(L + 1, KPoint{UINT32_MAX, 0.f, false});
+      std::copy(knn.begin(), knn.begin() + L, results.begin());
+    } else if (seq) {
+      for (unsigned l = 0; l < L; ++l) {
+        unsigned r = insert_knn_seq(&results[0], (unsigned)results.size() - 1, knn[l]);
+        if (r < results.size() && results.size() < searchK + 1) results.push_back(KPoint{UINT32_MAX, 0.f, false});
+      }
+    } else {
+      for (unsigned l = 0; l < L; ++l) {
+        unsigned r = insert_knn_canon(&results[0], (unsigned)results.size() - 1, knn[l]);
+        if (r < results.size() && results.size() < searchK + 1) results.push_back(KPoint{UINT32_MAX, 0.f, false});
+      }
+    }
+  }
+  // :649-651; the slot past the live list holds an uninitialised Point in the reference: -1 here
+  for (uint32_t i = 0; i < searchK; i++) {
+    uint32_t id = i + 1 < results.size() ? results[i].id : UINT32_MAX;
+    out[i] = id == UINT32_MAX ? -1 : (int32_t)id;
+  }
   if (nd) *nd = evals;
 }
 
@@ -1507,6 +1644,38 @@ int orc_search(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* for
   for (long long i = 0; i < (long long)nq; ++i)
     search_one(X, *F, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, mode, seed, out + (uint64_t)i * k,
                evals ? evals + i : nullptr);
+  return 0;
+}
+
+// Batched kgraph search (getNeighbors_kgraph).  *init_num is the index's pool size; like the
+// reference (kdtreeub_index.hpp:510-514) it is raised to epochs * extend_to when that is not
+// smaller, and the raised value is written back for the caller's next search.
+int orc_search_kgraph(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* forest, const uint64_t* gptr,
+                      const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, int epochs, int* init_num,
+                      int extend_to, int search_trees, uint32_t k, int mode, int threads, uint64_t seed, int32_t* out,
+                      uint64_t* evals) {
+  Data X{data, n, d, ld, mode};
+  Forest* F = (Forest*)forest;
+  if (search_trees <= 0 || (size_t)search_trees > F->nodes.size()) return -1;
+  if (!init_num || *init_num <= 0 || epochs < 0 || extend_to < 0) return -1;
+  if (extend_to > *init_num) extend_to = *init_num;  // setSearchParams (base_index.hpp:156-157)
+  unsigned lsize = (unsigned)*init_num * 2 / (5 * (unsigned)search_trees) + 1;
+  unsigned pool_size = (unsigned)epochs * (unsigned)extend_to;
+  bool sorted = true;
+  if (pool_size >= (unsigned)*init_num) {
+    *init_num = (int)pool_size;
+    sorted = false;
+  }
+  if ((uint64_t)*init_num > n || *init_num <= 0) return -1;  // the reference's random fill would not end
+  SearchArgs a{epochs, *init_num, extend_to, search_trees, k};
+  if (mode == MODE_SEQ) srand(1);
+#ifdef _OPENMP
+  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+#endif
+  for (long long i = 0; i < (long long)nq; ++i)
+    search_one_kgraph(X, *F, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, lsize, sorted, mode, seed,
+                      out + (uint64_t)i * k, evals ? evals + i : nullptr);
   return 0;
 }
 

@@ -80,6 +80,9 @@ def lib():
         L.orc_search.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
                                  C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int,
                                  C.c_int, C.c_uint64, i32p, u64p]
+        L.orc_search_kgraph.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
+                                        C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                        C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p, u64p]
         _lib = L
     return _lib
 
@@ -223,3 +226,24 @@ def search(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, init_num=1
     if rc != 0:
         raise ValueError("orc_search rejected its arguments")
     return (out, ev) if want_evals else out
+
+
+def search_kgraph(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, init_num=1200, extend_to=200,
+                  trees=16, mode: int = CANON, threads: int = 1, seed: int = 1998):
+    """getNeighbors_kgraph.  Returns (ids, evals per query, pool size in effect afterwards): the
+    reference raises its stored pool size to epochs * extend_to when that is not smaller."""
+    data = np.ascontiguousarray(data, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    gptr = np.ascontiguousarray(gptr, np.uint64)
+    gids = np.ascontiguousarray(gids, np.uint32)
+    nq = queries.shape[0]
+    out = np.zeros((nq, k), np.int32)
+    ev = np.zeros(nq, np.uint64)
+    pool = C.c_int(init_num)
+    rc = lib().orc_search_kgraph(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1], forest.h,
+                                 _p(gptr, C.c_uint64), _p(gids, C.c_uint32), _p(queries, C.c_float), nq,
+                                 queries.shape[1], epochs, C.byref(pool), extend_to, trees, k, mode, threads, seed,
+                                 _p(out, C.c_int32), _p(ev, C.c_uint64))
+    if rc != 0:
+        raise ValueError("orc_search_kgraph rejected its arguments")
+    return out, ev, pool.value

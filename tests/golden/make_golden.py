@@ -10,6 +10,12 @@ across runs) on small seeded integer-valued data, and stores inputs and outputs:
   <case>.graph the reference's graph file, byte-for-byte
   ref_recall_100k.json  graph recall@10 of the reference's multi-threaded build at N=100k (3 runs
                + 1 single-thread run) against exact 10-NN, with build times on this host.
+  <case>_kgraph.npz  the reference's kgraph search (search method 1, through its FIndex API via
+               oracle/ref_drivers/kgraph_search.cc) on the case's trees and graph files, for each
+               parameter set in KGRAPH_POINTS: the first call's ids and a second call's ids on the
+               same index (the first call may enlarge the stored pool size).
+
+``--only-kgraph`` regenerates just the kgraph fixtures.
 
 The data are stored (as uint8) rather than regenerated so that the fixtures do not depend on the
 platform's numpy.
@@ -40,6 +46,12 @@ CASES = {
 }
 
 
+# kgraph search points (trees, epochs, pool, extend, k): sorted pools (epochs * extend < pool) and
+# pools the reference enlarges to epochs * extend.
+KGRAPH_POINTS = [(8, 4, 400, 50, 10), (8, 4, 100, 50, 10), (8, 3, 600, 40, 20), (4, 2, 150, 100, 10),
+                 (8, 5, 200, 30, 5)]
+
+
 def run(cmd, threads):
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     r = subprocess.run(cmd, env=env, capture_output=True, text=True)
@@ -63,6 +75,22 @@ def make_case(name, n, d, nq, gp, sp, tmp):
     res = io.read_ivecs(r)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), base=x.astype(np.uint8), queries=q.astype(np.uint8),
                         graph_params=np.array(gp), search_params=np.array(sp), results=res)
+
+
+def make_kgraph(name, tmp):
+    g = np.load(os.path.join(HERE, name + ".npz"))
+    base, qf, r = os.path.join(tmp, "b.fvecs"), os.path.join(tmp, "q.fvecs"), os.path.join(tmp, "r.ivecs")
+    io.write_fvecs(base, g["base"].astype(np.float32))
+    io.write_fvecs(qf, g["queries"].astype(np.float32))
+    first, second = [], []
+    for st, ep, pool, ext, k in KGRAPH_POINTS:
+        run([O.ref_bin("kgraph_search", "strict"), base, os.path.join(HERE, name + ".trees"),
+             os.path.join(HERE, name + ".graph"), qf, r, str(st), str(ep), str(pool), str(ext), str(k), "2"], 1)
+        first.append(io.read_ivecs(r))
+        second.append(io.read_ivecs(r + ".2"))
+    np.savez_compressed(os.path.join(HERE, name + "_kgraph.npz"), points=np.array(KGRAPH_POINTS),
+                        **{"first_%d" % i: a for i, a in enumerate(first)},
+                        **{"second_%d" % i: a for i, a in enumerate(second)})
 
 
 def exact_knn(x, k):
@@ -104,7 +132,10 @@ if __name__ == "__main__":
     if not O.build_ref():
         sys.exit("reference sources not found; fixtures unchanged")
     with tempfile.TemporaryDirectory() as tmp:
-        for name, spec in CASES.items():
-            make_case(name, *spec, tmp)
-        if "--skip-100k" not in sys.argv:
+        if "--only-kgraph" not in sys.argv:
+            for name, spec in CASES.items():
+                make_case(name, *spec, tmp)
+        for name in CASES:
+            make_kgraph(name, tmp)
+        if "--skip-100k" not in sys.argv and "--only-kgraph" not in sys.argv:
             ref_recall_100k(tmp)

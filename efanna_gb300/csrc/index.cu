@@ -302,6 +302,8 @@ void efg_index_destroy(efg_index* idx) {
   idx->ht_scratch.release();
   idx->ovf_list.release();
   idx->base16.release();
+  idx->kg_keys.release();
+  idx->kg_bits.release();
   if (idx->d_base) cudaFree(idx->d_base);
   if (idx->stream) cudaStreamDestroy(idx->stream);
   delete idx;

@@ -103,6 +103,9 @@ struct efg_index {
   int precision = 0;
   efg::DevBuf<uint16_t> base16;
   uint32_t ld16 = 0;
+  // kgraph search scratch: pool keys per query, visited bitsets per warp
+  efg::DevBuf<uint64_t> kg_keys;
+  efg::DevBuf<uint32_t> kg_bits;
 };
 
 namespace efg {
@@ -127,6 +130,9 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
                   cudaStream_t s, bool count_evals);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
+// kgraph.cu: search method 1 (getNeighbors_kgraph).
+int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
+                         cudaStream_t s, bool count_evals);
 
 // nndescent.cu
 struct NNDState;

@@ -30,7 +30,7 @@
 
 #include <cuda_bf16.h>
 
-#include "internal.cuh"
+#include "search.cuh"
 
 namespace efg {
 
@@ -44,25 +44,6 @@ static constexpr uint32_t EXPANDED = 0x80000000u;
 
 enum : uint32_t { SERR_FRONTIER = 1u, SERR_HASH = 2u };
 
-struct SearchCfg {
-  uint32_t T, lsize, init_num, extend_to, result_size, epochs, k;
-  uint32_t ht_size;     // visited-set slots
-  uint32_t ht_limit;    // inserts allowed before the query is handed to the overflow pass
-  uint32_t ht_global;   // visited set in a per-CTA slice of global scratch
-  uint32_t ids_cap;     // candidate id buffer (u32 entries)
-  uint32_t res_cap;     // power of two >= result_size
-  uint32_t nseq;        // T * lsize leaf slots
-  uint32_t tpw;         // trees per warp in the descent
-  // shared-memory byte offsets
-  uint32_t o_ids, o_ht, o_u;
-  uint32_t o_lstart, o_lend, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
-  uint32_t o_res, o_tmp, o_newk, o_surv;                // select phase (absolute)
-  uint32_t q4;          // staged query length in float4 (covers both row layouts)
-  // BF16 screening: rows ld16 values apart, cpr16 16-byte chunks per row, 2^gshift16 lanes per
-  // row in the gather; the first `rerank` results are re-scored in FP32 before the k are emitted
-  uint32_t bf16, ld16, cpr16, gshift16, rerank;
-  uint64_t seed;
-};
 
 __device__ __forceinline__ uint32_t ht_slot(uint32_t id, uint32_t size) { return __umulhi(id * 2654435761u, size); }
 
@@ -166,48 +147,53 @@ int make_base16(efg_index* idx) {
   return EFG_OK;
 }
 
-int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
-                  cudaStream_t s, bool count_evals) {
-  const SearchParams& sp = idx->sp;
-  if (sp.method != 0) return fail(EFG_ERR_ARG, "only search method 0 (nnexp) is implemented");
-  if (idx->forest.ntrees == 0) return fail(EFG_ERR_STATE, "no trees: build or load trees before searching");
-  if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
-  if (sp.search_trees <= 0) return fail(EFG_ERR_ARG, "search trees must be positive");
-  if ((uint32_t)sp.search_trees > idx->forest.ntrees) return fail(EFG_ERR_TREE_COUNT, "wrong tree number");
-  if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
-  if (k == 0 || (int)k > sp.init_num) return fail(EFG_ERR_ARG, "k must be in [1, pool size]");
-  if (sp.epochs < 0 || sp.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
-  if (nq == 0) return EFG_OK;
+__global__ void __launch_bounds__(512) row_sort_kernel(uint64_t* keys, uint32_t stride, uint32_t count,
+                                                       uint32_t p2) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* k = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* row = keys + (uint64_t)blockIdx.x * stride;
+  for (uint32_t i = threadIdx.x; i < p2; i += blockDim.x) k[i] = i < count ? row[i] : ~0ULL;
+  __syncthreads();
+  sort_keys_block(k, p2);
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) row[i] = k[i];
+}
 
-  SearchCfg cfg{};
-  cfg.T = (uint32_t)sp.search_trees;
-  cfg.lsize = (uint32_t)sp.init_num * 2 / (5 * cfg.T) + 1;
-  cfg.init_num = (uint32_t)sp.init_num;
-  cfg.extend_to = (uint32_t)sp.extend_to;
-  cfg.result_size = std::max<uint32_t>(cfg.extend_to, k);
-  cfg.epochs = (uint32_t)sp.epochs;
-  cfg.k = k;
-  cfg.seed = idx->bp.seed;
-  cfg.nseq = cfg.T * cfg.lsize;
-  if (idx->precision == EFG_PRECISION_BF16) {
-    if (!idx->base16.p) EFG_TRY(make_base16(idx));
-    cfg.bf16 = 1;
-    cfg.ld16 = idx->ld16;
-    cfg.cpr16 = idx->ld16 / 8;
-    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr16), 32);
-    while ((1u << cfg.gshift16) < g) ++cfg.gshift16;
-    cfg.rerank = std::min<uint32_t>(std::min<uint32_t>(std::max(2 * k, k + 32), cfg.result_size),
-                                    (uint32_t)SEL_CHUNK);
-    if (k > cfg.rerank) return fail(EFG_ERR_ARG, "k above 1024 is not supported with BF16 screening");
+int launch_row_sort(uint64_t* keys, uint64_t nq, uint32_t stride, uint32_t count, cudaStream_t s) {
+  if (nq == 0 || count < 2) return EFG_OK;
+  if (count > 16384) return fail(EFG_ERR_ARG, "kgraph search: pools above 16384 are not supported");
+  uint32_t p2 = next_pow2(count);
+  size_t smem = (size_t)p2 * 8;
+  EFG_CUDA(cudaFuncSetAttribute(row_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for (uint64_t q0 = 0; q0 < nq; q0 += 65535) {
+    uint64_t m = std::min<uint64_t>(nq - q0, 65535);
+    row_sort_kernel<<<(unsigned)m, 512, smem, s>>>(keys + q0 * stride, stride, count, p2);
+    EFG_CUDA(cudaGetLastError());
   }
-  if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
-  if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
+  return EFG_OK;
+}
+
+// Largest graph row length (the fixed degree when every row has K ids).
+uint32_t graph_max_degree(efg_index* idx) {
   uint32_t maxdeg = idx->graph.fixed_k;
   if (!maxdeg) {
     std::vector<uint64_t> ptr(idx->graph.n + 1);
-    EFG_CUDA(cudaMemcpy(ptr.data(), idx->graph.ptr.p, ptr.size() * 8, cudaMemcpyDeviceToHost));
+    cudaMemcpy(ptr.data(), idx->graph.ptr.p, ptr.size() * 8, cudaMemcpyDeviceToHost);
     for (uint64_t i = 0; i < idx->graph.n; ++i) maxdeg = std::max<uint32_t>(maxdeg, (uint32_t)(ptr[i + 1] - ptr[i]));
   }
+  return maxdeg;
+}
+
+// Launches the nnexp kernel for cfg's search parameters (T, lsize, init_num, extend_to,
+// result_size, epochs, k, seed, nseq and the precision fields set) over nq queries: a first pass
+// with visited sets in shared memory and, when the worst case does not fit there, an overflow
+// pass for the queries that outgrew them.  With d_keys set the kernel stops after the pool and
+// writes each query's init_num packed (dist, id) keys in pool order instead of ids.
+int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
+                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches) {
+  *launches = 0;
+  if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
+  if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
+  cfg.emit_pool = d_keys ? 1 : 0;
   // visited set: shared memory sized for the expected visits; worst case in global memory
   uint64_t worst = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg;
   uint64_t expect = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg / 4;
@@ -244,8 +230,6 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
     return fail(EFG_ERR_ARG, "search parameters need " + std::to_string(smem1) +
                                  " bytes of shared memory per query (pool/extend/degree too large)");
   EFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(smem1, smem2)));
-  EFG_TRY(idx->eval_counter.reserve(3));
-  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 24, s));
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -258,50 +242,105 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
     EFG_TRY(idx->ovf_list.reserve(nq + 1));
     EFG_CUDA(cudaMemsetAsync(idx->ovf_list.p, 0, 4, s));
   }
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, s);
   const Forest& F = idx->forest;
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
       idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
       idx->graph.ids.p, d_q, nq, qld, c1, d_out, idx->eval_counter.p, idx->ht_scratch.p, nullptr,
-      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p);
+      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys);
   cudaError_t le = cudaGetLastError();
+  *launches = 1;
   if (le == cudaSuccess && two_pass) {
     kernel<<<(unsigned)grid2, threads, smem2, s>>>(
         idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
         idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr,
-        idx->base16.p);
+        idx->base16.p, d_keys);
     le = cudaGetLastError();
+    *launches = 2;
   }
+  if (le != cudaSuccess) return fail(EFG_ERR_CUDA, std::string("nnexp launch: ") + cudaGetErrorString(le));
+  return EFG_OK;
+}
+
+// Search parameters common to both methods: checks and the tree-descent fields of the config.
+int search_common_checks(efg_index* idx, uint32_t k) {
+  const SearchParams& sp = idx->sp;
+  if (idx->forest.ntrees == 0) return fail(EFG_ERR_STATE, "no trees: build or load trees before searching");
+  if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
+  if (sp.search_trees <= 0) return fail(EFG_ERR_ARG, "search trees must be positive");
+  if ((uint32_t)sp.search_trees > idx->forest.ntrees) return fail(EFG_ERR_TREE_COUNT, "wrong tree number");
+  if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
+  if (sp.epochs < 0 || sp.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
+  if (k == 0) return fail(EFG_ERR_ARG, "k must be positive");
+  return EFG_OK;
+}
+
+// Reads the per-call counters back into the index's search statistics.
+int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, uint64_t nq, bool two_pass,
+                        int launches, uint64_t reranked) {
+  unsigned long long h[3];
+  uint32_t novf = 0;
+  EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 24, cudaMemcpyDeviceToHost, s));
+  if (two_pass) EFG_CUDA(cudaMemcpyAsync(&novf, idx->ovf_list.p, 4, cudaMemcpyDeviceToHost, s));
+  EFG_CUDA(cudaStreamSynchronize(s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  idx->sstats.device_ms = ms;
+  idx->sstats.distance_evals = h[0];
+  idx->sstats.queries = nq;
+  idx->sstats.expanded_nodes = h[2];
+  idx->sstats.overflow_queries = novf;
+  idx->sstats.kernel_launches = (uint64_t)launches;
+  idx->sstats.reranked = reranked;
+  if (h[1] & SERR_FRONTIER) return fail(EFG_ERR_DEVICE_LIMIT, "tree descent frontier overflow");
+  if (h[1] & SERR_HASH) return fail(EFG_ERR_DEVICE_LIMIT, "candidate buffer overflow");
+  return EFG_OK;
+}
+
+int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
+                  cudaStream_t s, bool count_evals) {
+  const SearchParams& sp = idx->sp;
+  if (sp.method == 1) return kgraph_search_device(idx, d_q, nq, qld, k, d_out, s, count_evals);
+  if (sp.method != 0) return fail(EFG_ERR_ARG, "no such searching method");
+  EFG_TRY(search_common_checks(idx, k));
+  if ((int)k > sp.init_num) return fail(EFG_ERR_ARG, "k must be in [1, pool size]");
+  if (nq == 0) return EFG_OK;
+
+  SearchCfg cfg{};
+  cfg.T = (uint32_t)sp.search_trees;
+  cfg.lsize = (uint32_t)sp.init_num * 2 / (5 * cfg.T) + 1;
+  cfg.init_num = (uint32_t)sp.init_num;
+  cfg.extend_to = (uint32_t)sp.extend_to;
+  cfg.result_size = std::max<uint32_t>(cfg.extend_to, k);
+  cfg.epochs = (uint32_t)sp.epochs;
+  cfg.k = k;
+  cfg.seed = idx->bp.seed;
+  cfg.nseq = cfg.T * cfg.lsize;
+  if (idx->precision == EFG_PRECISION_BF16) {
+    if (!idx->base16.p) EFG_TRY(make_base16(idx));
+    cfg.bf16 = 1;
+    cfg.ld16 = idx->ld16;
+    cfg.cpr16 = idx->ld16 / 8;
+    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr16), 32);
+    while ((1u << cfg.gshift16) < g) ++cfg.gshift16;
+    cfg.rerank = std::min<uint32_t>(std::min<uint32_t>(std::max(2 * k, k + 32), cfg.result_size),
+                                    (uint32_t)SEL_CHUNK);
+    if (k > cfg.rerank) return fail(EFG_ERR_ARG, "k above 1024 is not supported with BF16 screening");
+  }
+  uint32_t maxdeg = graph_max_degree(idx);
+  EFG_TRY(idx->eval_counter.reserve(3));
+  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 24, s));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  int launches = 0;
+  int rc = launch_nnexp(idx, cfg, maxdeg, d_q, nq, qld, d_out, nullptr, s, &launches);
   cudaEventRecord(e1, s);
-  if (le != cudaSuccess) {
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return fail(EFG_ERR_CUDA, std::string("nnexp launch: ") + cudaGetErrorString(le));
-  }
-  if (count_evals) {
-    unsigned long long h[3];
-    uint32_t novf = 0;
-    EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 24, cudaMemcpyDeviceToHost, s));
-    if (two_pass) EFG_CUDA(cudaMemcpyAsync(&novf, idx->ovf_list.p, 4, cudaMemcpyDeviceToHost, s));
-    EFG_CUDA(cudaStreamSynchronize(s));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    idx->sstats.device_ms = ms;
-    idx->sstats.distance_evals = h[0];
-    idx->sstats.queries = nq;
-    idx->sstats.expanded_nodes = h[2];
-    idx->sstats.overflow_queries = novf;
-    idx->sstats.kernel_launches = two_pass ? 2 : 1;
-    idx->sstats.reranked = cfg.bf16 ? std::min<uint32_t>(cfg.rerank, cfg.result_size) : 0;
-    if (h[1] & SERR_FRONTIER) return fail(EFG_ERR_DEVICE_LIMIT, "tree descent frontier overflow");
-    if (h[1] & SERR_HASH) return fail(EFG_ERR_DEVICE_LIMIT, "candidate buffer overflow");
-  }
+  if (rc == EFG_OK && count_evals)
+    rc = finish_search_stats(idx, s, e0, e1, nq, launches == 2, launches, cfg.bf16 ? cfg.rerank : 0);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return EFG_OK;
+  return rc;
 }
 
 }  // namespace efg

@@ -1,0 +1,43 @@
+// Declarations shared by the two search methods (search.cu: nnexp; kgraph.cu: kgraph).
+#pragma once
+#include "internal.cuh"
+
+namespace efg {
+
+struct SearchCfg {
+  uint32_t T, lsize, init_num, extend_to, result_size, epochs, k;
+  uint32_t ht_size;     // visited-set slots
+  uint32_t ht_limit;    // inserts allowed before the query is handed to the overflow pass
+  uint32_t ht_global;   // visited set in a per-CTA slice of global scratch
+  uint32_t ids_cap;     // candidate id buffer (u32 entries)
+  uint32_t res_cap;     // power of two >= result_size
+  uint32_t nseq;        // T * lsize leaf slots
+  uint32_t tpw;         // trees per warp in the descent
+  // shared-memory byte offsets
+  uint32_t o_ids, o_ht, o_u;
+  uint32_t o_lstart, o_lend, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
+  uint32_t o_res, o_tmp, o_newk, o_surv;                // select phase (absolute)
+  uint32_t q4;          // staged query length in float4 (covers both row layouts)
+  // BF16 screening: rows ld16 values apart, cpr16 16-byte chunks per row, 2^gshift16 lanes per
+  // row in the gather; the first `rerank` results are re-scored in FP32 before the k are emitted
+  uint32_t bf16, ld16, cpr16, gshift16, rerank;
+  uint32_t emit_pool;   // stop after the pool and write its keys (kgraph's first stage)
+  uint64_t seed;
+};
+
+// Largest graph row length (the fixed degree when every row has K ids).
+uint32_t graph_max_degree(efg_index* idx);
+// Launches the nnexp kernel (one or two passes) for cfg's search parameters; with d_keys set it
+// writes each query's pool keys (init_num per query, pool order) instead of result ids.
+int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
+                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches);
+// Checks shared by both methods (trees, graph, tree count, pool size, k).
+int search_common_checks(efg_index* idx, uint32_t k);
+// Reads the per-call device counters into the index's search statistics.
+int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, uint64_t nq, bool two_pass,
+                        int launches, uint64_t reranked);
+// Sorts the first `count` keys of each of nq rows (rows `stride` keys apart) ascending in place;
+// count <= 16384.
+int launch_row_sort(uint64_t* keys, uint64_t nq, uint32_t stride, uint32_t count, cudaStream_t s);
+
+}  // namespace efg

@@ -194,6 +194,13 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
   cfg.emit_pool = d_keys ? 1 : 0;
+  cfg.fixed_k = idx->graph.fixed_k >= 2 ? idx->graph.fixed_k : 0;
+  if (cfg.fixed_k) {
+    // item r * K + c -> (r, c) by a multiply-high: exact while items * K < 2^32
+    uint64_t items = (uint64_t)cfg.extend_to * cfg.fixed_k;
+    if (items * cfg.fixed_k >= (1ull << 32)) cfg.fixed_k = 0;
+    else cfg.kmagic = (uint32_t)(((1ull << 32) + cfg.fixed_k - 1) / cfg.fixed_k);
+  }
   // visited set: shared memory sized for the expected visits; worst case in global memory
   uint64_t worst = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg;
   uint64_t expect = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg / 4;

@@ -12,16 +12,17 @@ struct SearchCfg {
   uint32_t ids_cap;     // candidate id buffer (u32 entries)
   uint32_t res_cap;     // power of two >= result_size
   uint32_t nseq;        // T * lsize leaf slots
-  uint32_t tpw;         // trees per warp in the descent
   // shared-memory byte offsets
   uint32_t o_ids, o_ht, o_u;
-  uint32_t o_lstart, o_lend, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
+  uint32_t o_lstart, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
   uint32_t o_res, o_tmp, o_newk, o_surv;                // select phase (absolute)
   uint32_t q4;          // staged query length in float4 (covers both row layouts)
   // BF16 screening: rows ld16 values apart, cpr16 16-byte chunks per row, 2^gshift16 lanes per
   // row in the gather; the first `rerank` results are re-scored in FP32 before the k are emitted
   uint32_t bf16, ld16, cpr16, gshift16, rerank;
   uint32_t emit_pool;   // stop after the pool and write its keys (kgraph's first stage)
+  uint32_t fixed_k;     // graph degree when every row has it (0: row pointers), and
+  uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices
   uint64_t seed;
 };
 

@@ -45,7 +45,7 @@ class BuildStats(C.Structure):
 class SearchStats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("distance_evals", C.c_uint64), ("queries", C.c_uint64),
                 ("expanded_nodes", C.c_uint64), ("overflow_queries", C.c_uint64),
-                ("kernel_launches", C.c_uint64), ("reranked", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("reranked", C.c_uint64), ("migrated_queries", C.c_uint64)]
 
 
 class HostState(C.Structure):

@@ -225,6 +225,7 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   SearchCfg c1 = cfg, c2 = cfg;
   size_t smem1 = layout(c1, idx->ld, maxdeg, false, (uint32_t)small);
   c1.ht_limit = (uint32_t)(small * 4 / 5);
+  c1.ht_soft = c1.ht_limit;
   size_t smem2 = layout(c2, idx->ld, maxdeg, true, (uint32_t)big);
   c2.ht_limit = (uint32_t)big;
   bool two_pass = big > small;
@@ -244,6 +245,15 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   uint64_t grid1 = std::min<uint64_t>(nq, (uint64_t)sms * std::max(1, per_sm));
   uint64_t grid2 = (uint64_t)sms;
   if (c1.ht_global) EFG_TRY(idx->ht_scratch.reserve(grid1 * c1.ht_size));
+  if (two_pass && !c1.ht_global && grid1 * big * 4 <= (1ull << 30)) {
+    // a query whose set holds 80% of the shared table at a phase boundary continues in a
+    // worst-case table in global scratch; only a set that reaches 90% within one phase is handed
+    // to the overflow pass
+    c1.ht_mig = 1;
+    c1.mig_size = (uint32_t)big;
+    c1.ht_limit = (uint32_t)(small * 9 / 10);
+    EFG_TRY(idx->ht_scratch.reserve(grid1 * big));
+  }
   if (two_pass) {
     EFG_TRY(idx->ht_scratch.reserve(grid2 * c2.ht_size));
     EFG_TRY(idx->ovf_list.reserve(nq + 1));
@@ -284,9 +294,9 @@ int search_common_checks(efg_index* idx, uint32_t k) {
 // Reads the per-call counters back into the index's search statistics.
 int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, uint64_t nq, bool two_pass,
                         int launches, uint64_t reranked) {
-  unsigned long long h[3];
+  unsigned long long h[4];
   uint32_t novf = 0;
-  EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 24, cudaMemcpyDeviceToHost, s));
+  EFG_CUDA(cudaMemcpyAsync(h, idx->eval_counter.p, 32, cudaMemcpyDeviceToHost, s));
   if (two_pass) EFG_CUDA(cudaMemcpyAsync(&novf, idx->ovf_list.p, 4, cudaMemcpyDeviceToHost, s));
   EFG_CUDA(cudaStreamSynchronize(s));
   float ms = 0;
@@ -298,6 +308,7 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
   idx->sstats.overflow_queries = novf;
   idx->sstats.kernel_launches = (uint64_t)launches;
   idx->sstats.reranked = reranked;
+  idx->sstats.migrated_queries = h[3];
   if (h[1] & SERR_FRONTIER) return fail(EFG_ERR_DEVICE_LIMIT, "tree descent frontier overflow");
   if (h[1] & SERR_HASH) return fail(EFG_ERR_DEVICE_LIMIT, "candidate buffer overflow");
   return EFG_OK;
@@ -334,8 +345,8 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
     if (k > cfg.rerank) return fail(EFG_ERR_ARG, "k above 1024 is not supported with BF16 screening");
   }
   uint32_t maxdeg = graph_max_degree(idx);
-  EFG_TRY(idx->eval_counter.reserve(3));
-  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 24, s));
+  EFG_TRY(idx->eval_counter.reserve(4));
+  EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 32, s));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -8,6 +8,9 @@ struct SearchCfg {
   uint32_t T, lsize, init_num, extend_to, result_size, epochs, k;
   uint32_t ht_size;     // visited-set slots
   uint32_t ht_limit;    // inserts allowed before the query is handed to the overflow pass
+  uint32_t ht_soft;     // at a phase boundary, a set holding this many ids moves to global scratch
+  uint32_t ht_mig;      // (when enabled) into a table of mig_size slots, the worst case
+  uint32_t mig_size;
   uint32_t ht_global;   // visited set in a per-CTA slice of global scratch
   uint32_t ids_cap;     // candidate id buffer (u32 entries)
   uint32_t res_cap;     // power of two >= result_size

@@ -74,6 +74,7 @@ typedef struct efg_search_stats {
   uint64_t overflow_queries; /* queries whose visited set outgrew shared memory (second pass)   */
   uint64_t kernel_launches;  /* search kernels launched by the last search call (1 or 2)         */
   uint64_t reranked;         /* FP32 re-rank distances per query under BF16 screening (0 in FP32) */
+  uint64_t migrated_queries; /* queries whose visited set moved from shared to global memory      */
 } efg_search_stats;
 
 typedef struct efg_index efg_index;

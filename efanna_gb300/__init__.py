@@ -48,6 +48,16 @@ class SearchStats(C.Structure):
                 ("kernel_launches", C.c_uint64), ("reranked", C.c_uint64), ("migrated_queries", C.c_uint64)]
 
 
+class QueryParams(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("init_num", C.c_int32), ("extend_to", C.c_int32), ("k", C.c_uint32)]
+
+
+def query_params(rows) -> np.ndarray:
+    """(epochs, pool, extend, k) rows -> a contiguous array laid out as efg_query_params."""
+    a = np.ascontiguousarray(np.asarray(rows, dtype=np.int64).reshape(-1, 4).astype(np.int32))
+    return a
+
+
 class HostState(C.Structure):
     _fields_ = [("n", C.c_uint64), ("L", C.c_uint32), ("cap", C.c_uint32),
                 ("pool_dist", C.POINTER(C.c_float)), ("pool_id", C.POINTER(C.c_uint32)),
@@ -120,6 +130,12 @@ def lib():
         "efg_l2_pairs": (i32, [vp, u64, u32, u64, vp, vp, u64, vp, vp]),
         "efg_brute_force_knn": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_knn_search_batch": (i32, [vp, f32p, u64, u32, u64, vp, u32, C.POINTER(C.c_int32)]),
+        "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
+        "efg_search_plan_create": (i32, [vp, u64, C.POINTER(QueryParams), f32p, u64, C.POINTER(vp)]),
+        "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
+        "efg_search_plan_threads": (i32, [vp]),
+        "efg_search_plan_destroy": (None, [vp]),
         "efg_nnd_init": (i32, [vp, C.POINTER(HostState)]),
         "efg_nnd_iterate": (i32, [vp, C.POINTER(HostState), u32, C.POINTER(C.c_uint64)]),
     }
@@ -213,6 +229,26 @@ class Index:
                                     out.ctypes.data_as(C.POINTER(C.c_int32))))
         return out
 
+    def knn_search_batch(self, queries: np.ndarray, params, k_max: int) -> np.ndarray:
+        """Per-query (epochs, pool, extend, k) rows; returns nq x k_max ids, -1 past each k."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        p = query_params(params)
+        out = np.zeros((q.shape[0], k_max), dtype=np.int32)
+        _check(lib().efg_knn_search_batch(self._h, _fp(q), q.shape[0], q.shape[1], q.shape[1],
+                                          C.c_void_p(p.ctypes.data), k_max,
+                                          out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def knn_search_batch_device(self, q_ptr: int, nq: int, row_stride: int, params_ptr: int, limits, out_ptr: int,
+                                nq_ptr: int = 0, stream: int = 0):
+        lim = QueryParams(*[int(v) for v in limits])
+        _check(lib().efg_knn_search_batch_device(self._h, C.c_void_p(q_ptr), nq, row_stride, C.c_void_p(params_ptr),
+                                                 C.byref(lim), C.c_void_p(out_ptr), C.c_void_p(nq_ptr or None),
+                                                 C.c_void_p(stream)))
+
+    def search_plan(self, capacity: int, limits, calib: np.ndarray | None = None) -> "SearchPlan":
+        return SearchPlan(self, capacity, limits, calib)
+
     def knn_search_device(self, k: int, q_ptr: int, nq: int, row_stride: int, out_ptr: int, stream: int = 0):
         _check(lib().efg_knn_search_device(self._h, C.c_void_p(q_ptr), nq, row_stride, k, C.c_void_p(out_ptr),
                                            C.c_void_p(stream)))
@@ -264,6 +300,44 @@ class Index:
         pairs = C.c_uint64()
         _check(lib().efg_nnd_iterate(self._h, C.byref(hs), it, C.byref(pairs)))
         return int(pairs.value)
+
+
+class SearchPlan:
+    """A captured batched search (efg_search_plan): run(queries, params) -> nq x limits.k ids."""
+
+    def __init__(self, index: "Index", capacity: int, limits, calib: np.ndarray | None = None):
+        self.index = index
+        self.limits = QueryParams(*[int(v) for v in limits])
+        h = C.c_void_p()
+        cq = None if calib is None else np.ascontiguousarray(calib, dtype=np.float32)
+        _check(lib().efg_search_plan_create(index._h, capacity, C.byref(self.limits),
+                                            None if cq is None else _fp(cq), 0 if cq is None else cq.shape[0],
+                                            C.byref(h)))
+        self._h = h
+
+    @property
+    def threads(self) -> int:
+        return lib().efg_search_plan_threads(self._h)
+
+    def run(self, queries: np.ndarray, params, out: np.ndarray | None = None) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        p = query_params(params)
+        if out is None:
+            out = np.zeros((q.shape[0], self.limits.k), dtype=np.int32)
+        _check(lib().efg_search_plan_run(self._h, _fp(q), q.shape[0], q.shape[1], C.c_void_p(p.ctypes.data),
+                                         out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().efg_search_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _host_state(st) -> HostState:

@@ -1,3 +1,4 @@
+#include <algorithm>
 // efg_index lifecycle, parameters, file formats and the C ABI front door.
 //
 // The file formats are the reference's (ZJULearning/efanna):
@@ -222,6 +223,8 @@ static int upload_graph(efg_index* idx, const std::vector<uint64_t>& ptr, const 
     for (uint64_t i = 0; i < g.n && fixed; ++i) fixed = (ptr[i + 1] - ptr[i]) == k0;
     if (fixed) g.fixed_k = (uint32_t)k0;
   }
+  g.max_deg = 0;
+  for (uint64_t i = 0; i < g.n; ++i) g.max_deg = std::max<uint32_t>(g.max_deg, (uint32_t)(ptr[i + 1] - ptr[i]));
   g.valid = true;
   return EFG_OK;
 }
@@ -303,6 +306,7 @@ void efg_index_destroy(efg_index* idx) {
   idx->ovf_list.release();
   idx->base16.release();
   idx->kg_keys.release();
+  idx->qp_buf.release();
   idx->kg_bits.release();
   if (idx->d_base) cudaFree(idx->d_base);
   if (idx->stream) cudaStreamDestroy(idx->stream);
@@ -366,6 +370,58 @@ int efg_knn_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_
   if (!idx || (!d_q && nq) || (!d_out && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   return search_device(idx, d_q, nq, row_stride, k, d_out, (cudaStream_t)stream, false);
+}
+
+int efg_knn_search_batch_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t row_stride,
+                                const efg_query_params* d_params, const efg_query_params* limits, int32_t* d_out,
+                                const uint32_t* d_nq, void* stream) {
+  if (!idx || !limits || ((!d_q || !d_params || !d_out) && nq)) return fail(EFG_ERR_ARG, "null argument");
+  if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
+  if (idx->sp.method != 0) return fail(EFG_ERR_ARG, "per-query parameters are supported by search method 0 only");
+  return search_device_ex(idx, d_q, nq, row_stride, *limits, d_params, d_nq, d_out, (cudaStream_t)stream, false);
+}
+
+int efg_knn_search_batch(efg_index* idx, const float* q, uint64_t nq, uint32_t dim, uint64_t row_stride,
+                         const efg_query_params* params, uint32_t k_max, int32_t* out_ids) {
+  if (!idx || ((!q || !params || !out_ids) && nq)) return fail(EFG_ERR_ARG, "null argument");
+  if (dim != idx->dim) return fail(EFG_ERR_ARG, "query dimension differs from the base");
+  if (row_stride < dim) return fail(EFG_ERR_ARG, "row_stride < dim");
+  if (idx->sp.method != 0) return fail(EFG_ERR_ARG, "per-query parameters are supported by search method 0 only");
+  if (k_max == 0) return fail(EFG_ERR_ARG, "k_max must be positive");
+  if (nq == 0) return EFG_OK;
+  efg_query_params lim{0, 1, 0, k_max};
+  for (uint64_t i = 0; i < nq; ++i) {
+    const efg_query_params& p = params[i];
+    if (p.init_num <= 0 || (uint64_t)p.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
+    if (p.epochs < 0 || p.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
+    if (p.k == 0 || p.k > k_max || (int)p.k > p.init_num) return fail(EFG_ERR_ARG, "k must be in [1, min(k_max, pool)]");
+    lim.epochs = std::max(lim.epochs, p.epochs);
+    lim.init_num = std::max(lim.init_num, p.init_num);
+    lim.extend_to = std::max(lim.extend_to, std::min(p.extend_to, p.init_num));
+  }
+  if ((int)k_max > lim.init_num) lim.k = (uint32_t)lim.init_num;
+  EFG_TRY(idx->q_buf.reserve(nq * idx->ld));
+  EFG_TRY(idx->out_buf.reserve(nq * (uint64_t)lim.k));
+  EFG_TRY(idx->qp_buf.reserve(nq));
+  EFG_CUDA(cudaMemsetAsync(idx->q_buf.p, 0, nq * idx->ld * sizeof(float), idx->stream));
+  EFG_CUDA(cudaMemcpy2DAsync(idx->q_buf.p, idx->ld * sizeof(float), q, row_stride * sizeof(float), dim * sizeof(float),
+                             nq, cudaMemcpyHostToDevice, idx->stream));
+  EFG_CUDA(cudaMemcpyAsync(idx->qp_buf.p, params, nq * sizeof(efg_query_params), cudaMemcpyHostToDevice,
+                           idx->stream));
+  EFG_TRY(search_device_ex(idx, idx->q_buf.p, nq, idx->ld, lim, idx->qp_buf.p, nullptr, idx->out_buf.p, idx->stream,
+                           true));
+  if (lim.k == k_max) {
+    EFG_CUDA(cudaMemcpyAsync(out_ids, idx->out_buf.p, nq * (uint64_t)k_max * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             idx->stream));
+  } else {  // every pool is smaller than k_max: rows of lim.k ids, padded with -1
+    EFG_CUDA(cudaMemcpy2DAsync(out_ids, k_max * sizeof(int32_t), idx->out_buf.p, lim.k * sizeof(int32_t),
+                               lim.k * sizeof(int32_t), nq, cudaMemcpyDeviceToHost, idx->stream));
+  }
+  EFG_CUDA(cudaStreamSynchronize(idx->stream));
+  if (lim.k != k_max)
+    for (uint64_t i = 0; i < nq; ++i)
+      for (uint32_t j = lim.k; j < k_max; ++j) out_ids[i * k_max + j] = -1;
+  return EFG_OK;
 }
 
 int efg_knn_search(efg_index* idx, const float* q, uint64_t nq, uint32_t dim, uint64_t row_stride, uint32_t k,

@@ -67,10 +67,11 @@ struct Forest {
 struct Graph {
   uint64_t n = 0, nnz = 0;
   uint32_t fixed_k = 0;  // 0 when rows have different lengths
+  uint32_t max_deg = 0;  // longest row
   DevBuf<uint64_t> ptr;  // n + 1
   DevBuf<uint32_t> ids;  // nnz
   bool valid = false;
-  void release() { ptr.release(); ids.release(); valid = false; n = nnz = 0; fixed_k = 0; }
+  void release() { ptr.release(); ids.release(); valid = false; n = nnz = 0; fixed_k = 0; max_deg = 0; }
 };
 
 struct SearchParams {
@@ -106,6 +107,8 @@ struct efg_index {
   // kgraph search scratch: pool keys per query, visited bitsets per warp
   efg::DevBuf<uint64_t> kg_keys;
   efg::DevBuf<uint32_t> kg_bits;
+  efg::DevBuf<efg_query_params> qp_buf;  // per-query parameters of a host batch
+  int search_threads = 0;                  // nnexp block size forced by a plan's autotuner (0: by occupancy)
 };
 
 namespace efg {
@@ -128,6 +131,11 @@ int download_forest(efg_index* idx, std::vector<HNode>& nodes, std::vector<uint3
 // search.cu
 int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                   cudaStream_t s, bool count_evals);
+// nnexp over a batch whose queries carry their own parameters (d_params, bounded by lim), or all
+// use lim when d_params is null; d_nq optionally holds the batch size on the device.
+int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
+                     const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
+                     bool count_evals);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
 // kgraph.cu: search method 1 (getNeighbors_kgraph).

@@ -276,6 +276,8 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
                          cudaStream_t s, bool count_evals) {
   SearchParams& sp = idx->sp;
   EFG_TRY(search_common_checks(idx, k));
+  if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
+  if (sp.epochs < 0 || sp.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
   const uint32_t T = (uint32_t)sp.search_trees, E = (uint32_t)sp.extend_to, epochs = (uint32_t)sp.epochs;
   const uint32_t lsize = (uint32_t)sp.init_num * 2 / (5 * T) + 1;  // from the pool size before it grows (:507)
   const uint64_t pool_size = (uint64_t)epochs * E;

@@ -952,6 +952,7 @@ int build_graph_device(efg_index* idx) {
   g.n = n;
   g.nnz = n * K;
   g.fixed_k = K;
+  g.max_deg = K;
   g.valid = true;
   float a = 0, b = 0, c = 0;
   cudaEventElapsedTime(&a, ev[0], ev[1]);

@@ -173,15 +173,7 @@ int launch_row_sort(uint64_t* keys, uint64_t nq, uint32_t stride, uint32_t count
 }
 
 // Largest graph row length (the fixed degree when every row has K ids).
-uint32_t graph_max_degree(efg_index* idx) {
-  uint32_t maxdeg = idx->graph.fixed_k;
-  if (!maxdeg) {
-    std::vector<uint64_t> ptr(idx->graph.n + 1);
-    cudaMemcpy(ptr.data(), idx->graph.ptr.p, ptr.size() * 8, cudaMemcpyDeviceToHost);
-    for (uint64_t i = 0; i < idx->graph.n; ++i) maxdeg = std::max<uint32_t>(maxdeg, (uint32_t)(ptr[i + 1] - ptr[i]));
-  }
-  return maxdeg;
-}
+uint32_t graph_max_degree(efg_index* idx) { return idx->graph.max_deg; }
 
 // Launches the nnexp kernel for cfg's search parameters (T, lsize, init_num, extend_to,
 // result_size, epochs, k, seed, nseq and the precision fields set) over nq queries: a first pass
@@ -189,7 +181,8 @@ uint32_t graph_max_degree(efg_index* idx) {
 // pass for the queries that outgrew them.  With d_keys set the kernel stops after the pool and
 // writes each query's init_num packed (dist, id) keys in pool order instead of ids.
 int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
-                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches) {
+                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches, const efg_query_params* d_params,
+                 const uint32_t* d_nq) {
   *launches = 0;
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
@@ -218,7 +211,8 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
                                   (int)std::min<size_t>(smem_probe, 227 * 1024)));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, s256::nnexp_kernel, 256, smem_probe);
   }
-  const bool wide = per_sm < 2;
+  // block size: the autotuned choice when one is set, else 256 threads when two CTAs fit on an SM
+  const bool wide = idx->search_threads ? idx->search_threads == 512 : per_sm < 2;
   const int threads = wide ? 512 : 256;
   auto kernel = wide ? s512::nnexp_kernel : s256::nnexp_kernel;
   auto layout = wide ? s512::layout : s256::layout;
@@ -263,14 +257,14 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
       idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
       idx->graph.ids.p, d_q, nq, qld, c1, d_out, idx->eval_counter.p, idx->ht_scratch.p, nullptr,
-      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys);
+      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys, d_params, d_nq);
   cudaError_t le = cudaGetLastError();
   *launches = 1;
   if (le == cudaSuccess && two_pass) {
     kernel<<<(unsigned)grid2, threads, smem2, s>>>(
         idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
         idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr,
-        idx->base16.p, d_keys);
+        idx->base16.p, d_keys, d_params, d_nq);
     le = cudaGetLastError();
     *launches = 2;
   }
@@ -285,8 +279,6 @@ int search_common_checks(efg_index* idx, uint32_t k) {
   if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
   if (sp.search_trees <= 0) return fail(EFG_ERR_ARG, "search trees must be positive");
   if ((uint32_t)sp.search_trees > idx->forest.ntrees) return fail(EFG_ERR_TREE_COUNT, "wrong tree number");
-  if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
-  if (sp.epochs < 0 || sp.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
   if (k == 0) return fail(EFG_ERR_ARG, "k must be positive");
   return EFG_OK;
 }
@@ -314,22 +306,24 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
   return EFG_OK;
 }
 
-int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
-                  cudaStream_t s, bool count_evals) {
+int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
+                     const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
+                     bool count_evals) {
   const SearchParams& sp = idx->sp;
-  if (sp.method == 1) return kgraph_search_device(idx, d_q, nq, qld, k, d_out, s, count_evals);
-  if (sp.method != 0) return fail(EFG_ERR_ARG, "no such searching method");
+  const uint32_t k = lim.k;
   EFG_TRY(search_common_checks(idx, k));
-  if ((int)k > sp.init_num) return fail(EFG_ERR_ARG, "k must be in [1, pool size]");
+  if (lim.init_num <= 0 || (uint64_t)lim.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
+  if (lim.epochs < 0 || lim.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
+  if ((int)k > lim.init_num) return fail(EFG_ERR_ARG, "k must be in [1, pool size]");
   if (nq == 0) return EFG_OK;
 
   SearchCfg cfg{};
   cfg.T = (uint32_t)sp.search_trees;
-  cfg.lsize = (uint32_t)sp.init_num * 2 / (5 * cfg.T) + 1;
-  cfg.init_num = (uint32_t)sp.init_num;
-  cfg.extend_to = (uint32_t)sp.extend_to;
+  cfg.lsize = (uint32_t)lim.init_num * 2 / (5 * cfg.T) + 1;
+  cfg.init_num = (uint32_t)lim.init_num;
+  cfg.extend_to = std::min<uint32_t>((uint32_t)lim.extend_to, cfg.init_num);
   cfg.result_size = std::max<uint32_t>(cfg.extend_to, k);
-  cfg.epochs = (uint32_t)sp.epochs;
+  cfg.epochs = (uint32_t)lim.epochs;
   cfg.k = k;
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
@@ -352,13 +346,22 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   int launches = 0;
-  int rc = launch_nnexp(idx, cfg, maxdeg, d_q, nq, qld, d_out, nullptr, s, &launches);
+  int rc = launch_nnexp(idx, cfg, maxdeg, d_q, nq, qld, d_out, nullptr, s, &launches, d_params, d_nq);
   cudaEventRecord(e1, s);
   if (rc == EFG_OK && count_evals)
     rc = finish_search_stats(idx, s, e0, e1, nq, launches == 2, launches, cfg.bf16 ? cfg.rerank : 0);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;
+}
+
+int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
+                  cudaStream_t s, bool count_evals) {
+  const SearchParams& sp = idx->sp;
+  if (sp.method == 1) return kgraph_search_device(idx, d_q, nq, qld, k, d_out, s, count_evals);
+  if (sp.method != 0) return fail(EFG_ERR_ARG, "no such searching method");
+  efg_query_params lim{sp.epochs, sp.init_num, sp.extend_to, k};
+  return search_device_ex(idx, d_q, nq, qld, lim, nullptr, nullptr, d_out, s, count_evals);
 }
 
 }  // namespace efg

@@ -34,9 +34,11 @@ uint32_t graph_max_degree(efg_index* idx);
 // Launches the nnexp kernel (one or two passes) for cfg's search parameters; with d_keys set it
 // writes each query's pool keys (init_num per query, pool order) instead of result ids.
 int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
-                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches);
+                 int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches,
+                 const efg_query_params* d_params = nullptr, const uint32_t* d_nq = nullptr);
 // Checks shared by both methods (trees, graph, tree count, pool size, k).
 int search_common_checks(efg_index* idx, uint32_t k);
+
 // Reads the per-call device counters into the index's search statistics.
 int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, uint64_t nq, bool two_pass,
                         int launches, uint64_t reranked);

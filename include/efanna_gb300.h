@@ -125,6 +125,44 @@ int efg_knn_search_device(efg_index* idx, const float* d_queries, uint64_t nq, u
                           uint32_t k, int32_t* d_out_ids, void* stream);
 int efg_get_search_stats(const efg_index* idx, efg_search_stats* out);
 
+/* Batching form (no reference counterpart: the reference applies one setSearchParams to a whole
+ * batch).  Each query carries its own nnexp parameters; extend_to is clamped to init_num and k to
+ * [1, init_num].  Method 0 (nnexp) with the index's search_trees and precision. */
+typedef struct efg_query_params {
+  int32_t epochs;
+  int32_t init_num;  /* pool size */
+  int32_t extend_to;
+  uint32_t k;
+} efg_query_params;
+/* Host arrays: params has nq entries (init_num in [1, n], k in [1, k_max]); out_ids receives nq
+ * rows of k_max ids, -1 past a query's k. */
+int efg_knn_search_batch(efg_index* idx, const float* queries, uint64_t nq, uint32_t dim, uint64_t row_stride,
+                         const efg_query_params* params, uint32_t k_max, int32_t* out_ids);
+/* Device arrays: d_params (nq entries) and d_out_ids (nq rows of limits->k ids) in device memory;
+ * `limits` (host memory) bounds every query's parameters -- larger values are clamped to it -- and
+ * sizes the launch.  Runs on `stream` without synchronising.  d_nq, when not NULL, is a device
+ * counter read by the kernel in place of nq (nq is then the capacity): a launch sequence captured
+ * once in a CUDA graph serves batches of any size up to nq. */
+int efg_knn_search_batch_device(efg_index* idx, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                                const efg_query_params* d_params, const efg_query_params* limits,
+                                int32_t* d_out_ids, const uint32_t* d_nq, void* stream);
+
+/* A search plan: the batched nnexp launch sequence for up to `capacity` queries whose parameters
+ * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers.  When
+ * calibration queries are given (n_calib > 0, host memory, dim floats per row), the plan's
+ * autotuner times the 256- and 512-thread kernel builds on them with the limits' parameters and
+ * keeps the faster.  efg_search_plan_run copies a batch in (queries, per-query parameters), replays
+ * the graph and copies nq rows of limits->k ids out.  A plan belongs to its index: the index must
+ * outlive it and must not be searched by other calls while a run is in progress. */
+typedef struct efg_search_plan efg_search_plan;
+int efg_search_plan_create(efg_index* idx, uint64_t capacity, const efg_query_params* limits,
+                           const float* calib_queries, uint64_t n_calib, efg_search_plan** out);
+int efg_search_plan_run(efg_search_plan* plan, const float* queries, uint64_t nq, uint64_t row_stride,
+                        const efg_query_params* params, int32_t* out_ids);
+/* Block size the autotuner chose (256 or 512; 0 when the plan chose by occupancy). */
+int efg_search_plan_threads(const efg_search_plan* plan);
+void efg_search_plan_destroy(efg_search_plan* plan);
+
 /* File I/O, byte-compatible with the reference's formats. */
 int efg_save_graph(efg_index* idx, const char* path);   /* saveGraph  kdtreeub_index.hpp:295-312 */
 int efg_load_graph(efg_index* idx, const char* path);   /* loadGraph  kdtreeub_index.hpp:243-277 */

@@ -132,6 +132,7 @@ def lib():
         "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_knn_search_batch": (i32, [vp, f32p, u64, u32, u64, vp, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
+        "efg_knn_search_seeded_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, u32, vp, vp]),
         "efg_search_plan_create": (i32, [vp, u64, C.POINTER(QueryParams), f32p, u64, C.POINTER(vp)]),
         "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_threads": (i32, [vp]),
@@ -245,6 +246,14 @@ class Index:
         _check(lib().efg_knn_search_batch_device(self._h, C.c_void_p(q_ptr), nq, row_stride, C.c_void_p(params_ptr),
                                                  C.byref(lim), C.c_void_p(out_ptr), C.c_void_p(nq_ptr or None),
                                                  C.c_void_p(stream)))
+
+    def knn_search_seeded_device(self, q_ptr: int, nq: int, row_stride: int, params_ptr: int, limits, seeds_ptr: int,
+                                 seeds_per_query: int, out_ptr: int, stream: int = 0):
+        lim = QueryParams(*[int(v) for v in limits])
+        _check(lib().efg_knn_search_seeded_device(self._h, C.c_void_p(q_ptr), nq, row_stride,
+                                                  C.c_void_p(params_ptr or None), C.byref(lim),
+                                                  C.c_void_p(seeds_ptr), seeds_per_query, C.c_void_p(out_ptr),
+                                                  C.c_void_p(stream)))
 
     def search_plan(self, capacity: int, limits, calib: np.ndarray | None = None) -> "SearchPlan":
         return SearchPlan(self, capacity, limits, calib)

@@ -381,6 +381,16 @@ int efg_knn_search_batch_device(efg_index* idx, const float* d_q, uint64_t nq, u
   return search_device_ex(idx, d_q, nq, row_stride, *limits, d_params, d_nq, d_out, (cudaStream_t)stream, false);
 }
 
+int efg_knn_search_seeded_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t row_stride,
+                                 const efg_query_params* d_params, const efg_query_params* limits,
+                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int32_t* d_out, void* stream) {
+  if (!idx || !limits || ((!d_q || !d_out || (!d_seeds && seeds_per_query)) && nq)) return fail(EFG_ERR_ARG, "null argument");
+  if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
+  if (idx->sp.method != 0) return fail(EFG_ERR_ARG, "seeded search uses search method 0");
+  return search_device_ex(idx, d_q, nq, row_stride, *limits, d_params, nullptr, d_out, (cudaStream_t)stream, false,
+                          d_seeds, seeds_per_query);
+}
+
 int efg_knn_search_batch(efg_index* idx, const float* q, uint64_t nq, uint32_t dim, uint64_t row_stride,
                          const efg_query_params* params, uint32_t k_max, int32_t* out_ids) {
   if (!idx || ((!q || !params || !out_ids) && nq)) return fail(EFG_ERR_ARG, "null argument");

@@ -56,9 +56,10 @@ struct Forest {
   DevBuf<int32_t> n_left, n_right, n_level, n_tree;
   DevBuf<uint32_t> n_start, n_end;
   DevBuf<int32_t> nleaf;                // leaves in each node's subtree (search descent ranks)
+  DevBuf<uint2> cnl;                    // per internal node: (nleaf[left], nleaf[right]), loaded with the node
   bool has_soa = false;
   void release() {
-    nodes.release(); d_roots.release(); leaves.release(); nleaf.release();
+    nodes.release(); d_roots.release(); leaves.release(); nleaf.release(); cnl.release();
     n_left.release(); n_right.release(); n_level.release(); n_tree.release(); n_start.release(); n_end.release();
     ntrees = 0; nnodes = 0; roots.clear(); has_soa = false;
   }
@@ -135,7 +136,7 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
 // use lim when d_params is null; d_nq optionally holds the batch size on the device.
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
-                     bool count_evals);
+                     bool count_evals, const uint32_t* d_seeds = nullptr, uint32_t seeds_per_query = 0);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
 // kgraph.cu: search method 1 (getNeighbors_kgraph).

@@ -116,7 +116,7 @@ __device__ __forceinline__ float warp_row_dists(const float4* qv, uint32_t ld4, 
   return mine;
 }
 
-__global__ void __launch_bounds__(KG_WARPS * 32) kgraph_kernel(
+__global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
     const float* __restrict__ base, uint32_t dim, uint32_t ld, const uint64_t* __restrict__ gptr,
     const uint32_t* __restrict__ gids, const float* __restrict__ queries, uint64_t nq, uint64_t qld,
     const uint64_t* __restrict__ keys, KgCfg c, int32_t* __restrict__ out, uint32_t* __restrict__ bits,

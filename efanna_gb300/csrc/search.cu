@@ -116,11 +116,13 @@ __device__ void sort_keys_block(uint64_t* keys, uint32_t n) {
 namespace s256 {
 static constexpr int S_THREADS = 256;
 static constexpr int S_WARPS = S_THREADS / 32;
+static constexpr int S_MIN_BLOCKS = 2;  // two CTAs per SM: at most 128 registers per thread
 #include "search_kernel.inc"
 }  // namespace s256
 namespace s512 {
 static constexpr int S_THREADS = 512;
 static constexpr int S_WARPS = S_THREADS / 32;
+static constexpr int S_MIN_BLOCKS = 1;
 #include "search_kernel.inc"
 }  // namespace s512
 
@@ -182,7 +184,7 @@ uint32_t graph_max_degree(efg_index* idx) { return idx->graph.max_deg; }
 // writes each query's init_num packed (dist, id) keys in pool order instead of ids.
 int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
                  int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches, const efg_query_params* d_params,
-                 const uint32_t* d_nq) {
+                 const uint32_t* d_nq, const uint32_t* d_seeds) {
   *launches = 0;
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
@@ -255,16 +257,16 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   }
   const Forest& F = idx->forest;
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
-      idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
+      idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.cnl.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
       idx->graph.ids.p, d_q, nq, qld, c1, d_out, idx->eval_counter.p, idx->ht_scratch.p, nullptr,
-      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys, d_params, d_nq);
+      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys, d_params, d_nq, d_seeds);
   cudaError_t le = cudaGetLastError();
   *launches = 1;
   if (le == cudaSuccess && two_pass) {
     kernel<<<(unsigned)grid2, threads, smem2, s>>>(
-        idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
+        idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.cnl.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
         idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr,
-        idx->base16.p, d_keys, d_params, d_nq);
+        idx->base16.p, d_keys, d_params, d_nq, d_seeds);
     le = cudaGetLastError();
     *launches = 2;
   }
@@ -308,7 +310,7 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
 
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
-                     bool count_evals) {
+                     bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query) {
   const SearchParams& sp = idx->sp;
   const uint32_t k = lim.k;
   EFG_TRY(search_common_checks(idx, k));
@@ -327,6 +329,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
   cfg.k = k;
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
+  cfg.nseeds = d_seeds ? seeds_per_query : 0;
   if (idx->precision == EFG_PRECISION_BF16) {
     if (!idx->base16.p) EFG_TRY(make_base16(idx));
     cfg.bf16 = 1;
@@ -346,7 +349,8 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   int launches = 0;
-  int rc = launch_nnexp(idx, cfg, maxdeg, d_q, nq, qld, d_out, nullptr, s, &launches, d_params, d_nq);
+  int rc = launch_nnexp(idx, cfg, maxdeg, d_q, nq, qld, d_out, nullptr, s, &launches, d_params, d_nq,
+                        cfg.nseeds ? d_seeds : nullptr);
   cudaEventRecord(e1, s);
   if (rc == EFG_OK && count_evals)
     rc = finish_search_stats(idx, s, e0, e1, nq, launches == 2, launches, cfg.bf16 ? cfg.rerank : 0);

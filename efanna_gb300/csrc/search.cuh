@@ -26,6 +26,7 @@ struct SearchCfg {
   uint32_t emit_pool;   // stop after the pool and write its keys (kgraph's first stage)
   uint32_t fixed_k;     // graph degree when every row has it (0: row pointers), and
   uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices
+  uint32_t nseeds;      // entry seeds per query placed ahead of the leaves (learned form)
   uint64_t seed;
 };
 
@@ -35,7 +36,8 @@ uint32_t graph_max_degree(efg_index* idx);
 // writes each query's pool keys (init_num per query, pool order) instead of result ids.
 int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_q, uint64_t nq, uint64_t qld,
                  int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches,
-                 const efg_query_params* d_params = nullptr, const uint32_t* d_nq = nullptr);
+                 const efg_query_params* d_params = nullptr, const uint32_t* d_nq = nullptr,
+                 const uint32_t* d_seeds = nullptr);
 // Checks shared by both methods (trees, graph, tree count, pool size, k).
 int search_common_checks(efg_index* idx, uint32_t k);
 

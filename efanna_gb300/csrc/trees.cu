@@ -292,6 +292,15 @@ __global__ void to_dnodes_kernel(NodeArrays na, uint32_t nnodes, DNode* __restri
 }
 
 // Leaves per subtree for the nodes [lo, hi) of one level; deeper levels are already done.
+// Children's leaf counts next to each node, so that the search descent gets them with the node.
+__global__ void child_counts_kernel(const DNode* __restrict__ nodes, const int32_t* __restrict__ nleaf, uint32_t m,
+                                    uint2* __restrict__ cnl) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= m) return;
+  DNode d = nodes[v];
+  cnl[v] = d.left < 0 ? make_uint2(0, 0) : make_uint2((uint32_t)nleaf[d.left], (uint32_t)nleaf[d.right]);
+}
+
 __global__ void leaf_count_kernel(const int32_t* __restrict__ left, const int32_t* __restrict__ right, int32_t lo,
                                   int32_t hi, int32_t* __restrict__ nleaf) {
   int32_t v = lo + (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -413,6 +422,8 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
     int32_t lo = level_ranges[l].first, hi = level_ranges[l].second;
     if (hi > lo) leaf_count_kernel<<<(hi - lo + 255) / 256, 256, 0, s>>>(na.left, na.right, lo, hi, F.nleaf.p);
   }
+  EFG_TRY(F.cnl.reserve(nnodes));
+  child_counts_kernel<<<(nnodes + 255) / 256, 256, 0, s>>>(F.nodes.p, F.nleaf.p, (uint32_t)nnodes, F.cnl.p);
   EFG_CUDA(cudaGetLastError());
   // keep dim/val in the DNode array; the SoA start/end/tree/level/left/right stay for the merge
   EFG_TRY(F.d_roots.reserve(ntrees));
@@ -506,6 +517,10 @@ int upload_forest(efg_index* idx, const std::vector<HNode>& nodes, const std::ve
   EFG_TRY(F.n_start.reserve(m));
   EFG_TRY(F.n_end.reserve(m));
   EFG_CUDA(cudaMemcpy(F.nodes.p, dn.data(), m * sizeof(DNode), cudaMemcpyHostToDevice));
+  EFG_TRY(F.cnl.reserve(m));
+  child_counts_kernel<<<(unsigned)((m + 255) / 256), 256>>>(F.nodes.p, F.nleaf.p, (uint32_t)m, F.cnl.p);
+  EFG_CUDA(cudaGetLastError());
+  EFG_CUDA(cudaStreamSynchronize(0));  // searches run on a non-blocking stream
   EFG_CUDA(cudaMemcpy(F.d_roots.p, roots.data(), ntrees * 4, cudaMemcpyHostToDevice));
   EFG_CUDA(cudaMemcpy(F.leaves.p, leaves.data(), leaves.size() * 4, cudaMemcpyHostToDevice));
   EFG_CUDA(cudaMemcpy(F.n_left.p, l.data(), m * 4, cudaMemcpyHostToDevice));

@@ -27,10 +27,15 @@ def _mixture_params(d: int, n_comp: int, seed: int):
 
 
 def mixture_u8(n: int, d: int = 128, n_comp: int = 64, seed: int = 0, queries: bool = False,
-               chunk: int = 1 << 18) -> np.ndarray:
-    """``n`` x ``d`` float32 integer-valued vectors of the seeded Gaussian mixture."""
+               chunk: int = 1 << 18, sample_seed: int | None = None) -> np.ndarray:
+    """``n`` x ``d`` float32 integer-valued vectors of the seeded Gaussian mixture.  With
+    ``sample_seed`` the draws come from that seed (a further held-out sample of the same mixture,
+    e.g. training queries)."""
     prng, w, centres, sigma = _mixture_params(d, n_comp, seed)
-    rng = np.random.default_rng(seed + 1) if queries else prng
+    if sample_seed is not None:
+        rng = np.random.default_rng(sample_seed)
+    else:
+        rng = np.random.default_rng(seed + 1) if queries else prng
     out = np.empty((n, d), dtype=np.float32)
     for s in range(0, n, chunk):
         e = min(n, s + chunk)

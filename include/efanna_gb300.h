@@ -147,6 +147,15 @@ int efg_knn_search_batch_device(efg_index* idx, const float* d_queries, uint64_t
                                 const efg_query_params* d_params, const efg_query_params* limits,
                                 int32_t* d_out_ids, const uint32_t* d_nq, void* stream);
 
+/* Seeded batch (the learned form's search): like efg_knn_search_batch_device, and each query's pool
+ * starts with its seeds_per_query entry ids from d_seeds (row qi, in order; ids >= n and repeats are
+ * skipped), followed by the tree leaves as usual until the query's pool size.  d_params may be NULL
+ * (every query at *limits). */
+int efg_knn_search_seeded_device(efg_index* idx, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                                 const efg_query_params* d_params, const efg_query_params* limits,
+                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int32_t* d_out_ids,
+                                 void* stream);
+
 /* A search plan: the batched nnexp launch sequence for up to `capacity` queries whose parameters
  * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers.  When
  * calibration queries are given (n_calib > 0, host memory, dim floats per row), the plan's

@@ -1253,6 +1253,8 @@ static void search_node_list(const Forest& F, unsigned t, int32_t ni, const floa
 struct SearchArgs {
   int epochs, init_num, extend_to, trees;
   uint32_t k;
+  const uint32_t* seeds = nullptr;  // this query's entry seeds (learned form)
+  unsigned nseeds = 0;
 };
 
 // Pool seeding shared by both search methods (kdtreeub_index.hpp:380-418 and :519-548): leaves of
@@ -1261,12 +1263,20 @@ struct SearchArgs {
 // per-query counter hash in canonical mode).  tbflag marks the pool's ids.
 static std::vector<int> fill_pool(const Data& X, const Forest& F, const float* q, uint64_t qi, unsigned T,
                                   unsigned lsize, unsigned init_num, int mode, uint64_t seed,
-                                  std::vector<uint8_t>& tbflag) {
+                                  std::vector<uint8_t>& tbflag, const uint32_t* seeds = nullptr,
+                                  unsigned nseeds = 0) {
   size_t N = X.n;
   std::vector<std::vector<int32_t>> cand(T);
   for (unsigned t = 0; t < T; ++t) search_node_list(F, t, F.roots[t], q, lsize, cand[t]);
   std::vector<int> pool(init_num);
   unsigned pcount = 0;
+  // entry seeds (learned form; no reference counterpart) ahead of the leaves, in order
+  for (unsigned j = 0; j < nseeds && pcount < init_num; ++j) {
+    uint32_t id = seeds[j];
+    if (id >= N || tbflag[id]) continue;
+    tbflag[id] = 1;
+    pool[pcount++] = (int)id;
+  }
   for (unsigned ni = 0; ni < lsize; ni++) {
     for (unsigned t = 0; t < T; t++) {
       if (ni >= cand[t].size()) continue;
@@ -1307,7 +1317,8 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
   std::vector<uint8_t> tbflag(N, 0), newflag(N, 1);
   unsigned T = (unsigned)a.trees;
   unsigned lsize = a.init_num * 2 / (5 * T) + 1;
-  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, tbflag);
+  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, tbflag, a.seeds,
+                                    a.nseeds);
   unsigned resultSize = (unsigned)a.extend_to;
   if (a.k > resultSize) resultSize = a.k;
   std::vector<std::pair<float, size_t>> result;
@@ -1644,6 +1655,34 @@ int orc_search(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* for
   for (long long i = 0; i < (long long)nq; ++i)
     search_one(X, *F, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, mode, seed, out + (uint64_t)i * k,
                evals ? evals + i : nullptr);
+  return 0;
+}
+
+// Batched nnexp search with per-query parameters (params: nq rows of epochs, pool, extend, k; out rows
+// of k_max ids, -1 past each k) and optional entry seeds (nq rows of seeds_per_query ids).
+int orc_search_batch(const float* data, uint64_t n, uint32_t d, uint64_t ld, void* forest, const uint64_t* gptr,
+                     const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, const int32_t* params,
+                     uint32_t k_max, int search_trees, const uint32_t* seeds, uint32_t seeds_per_query, int threads,
+                     uint64_t seed, int32_t* out) {
+  Data X{data, n, d, ld, MODE_CANON};
+  Forest* F = (Forest*)forest;
+  if (search_trees <= 0 || (size_t)search_trees > F->nodes.size()) return -1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads < 1 ? 1 : threads)
+#endif
+  for (long long i = 0; i < (long long)nq; ++i) {
+    const int32_t* p = params + 4 * i;
+    int init = p[1], ext = p[2] > p[1] ? p[1] : p[2];
+    uint32_t k = (uint32_t)p[3];
+    SearchArgs a{p[0], init, ext, search_trees, k};
+    if (seeds) {
+      a.seeds = seeds + (uint64_t)i * seeds_per_query;
+      a.nseeds = seeds_per_query;
+    }
+    std::vector<int32_t> row(k);
+    search_one(X, *F, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, MODE_CANON, seed, row.data(), nullptr);
+    for (uint32_t j = 0; j < k_max; ++j) out[(uint64_t)i * k_max + j] = j < k ? row[j] : -1;
+  }
   return 0;
 }
 

@@ -80,6 +80,9 @@ def lib():
         L.orc_search.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
                                  C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int,
                                  C.c_int, C.c_uint64, i32p, u64p]
+        L.orc_search_batch.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
+                                       C.c_uint64, C.c_uint64, i32p, C.c_uint32, C.c_int, u32p, C.c_uint32, C.c_int,
+                                       C.c_uint64, i32p]
         L.orc_search_kgraph.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
                                         C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
                                         C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p, u64p]
@@ -226,6 +229,27 @@ def search(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, init_num=1
     if rc != 0:
         raise ValueError("orc_search rejected its arguments")
     return (out, ev) if want_evals else out
+
+
+def search_batch(data, forest: Forest, gptr, gids, queries, params, k_max, trees=16, seeds=None, threads=1,
+                 seed: int = 1998):
+    """Canonical nnexp with per-query (epochs, pool, extend, k) rows and optional entry seeds."""
+    data = np.ascontiguousarray(data, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    gptr = np.ascontiguousarray(gptr, np.uint64)
+    gids = np.ascontiguousarray(gids, np.uint32)
+    params = np.ascontiguousarray(params, np.int32).reshape(-1, 4)
+    nq = queries.shape[0]
+    out = np.zeros((nq, k_max), np.int32)
+    sp = None if seeds is None else np.ascontiguousarray(seeds, np.uint32).reshape(nq, -1)
+    rc = lib().orc_search_batch(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1], forest.h,
+                                _p(gptr, C.c_uint64), _p(gids, C.c_uint32), _p(queries, C.c_float), nq,
+                                queries.shape[1], _p(params, C.c_int32), k_max, trees,
+                                None if sp is None else _p(sp, C.c_uint32), 0 if sp is None else sp.shape[1],
+                                threads, seed, _p(out, C.c_int32))
+    if rc != 0:
+        raise ValueError("orc_search_batch rejected its arguments")
+    return out
 
 
 def search_kgraph(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, init_num=1200, extend_to=200,

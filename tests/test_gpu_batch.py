@@ -102,3 +102,36 @@ def test_batch_argument_errors(efg, setup):
         idx.knn_search_batch(q[:1], [(4, 0, 100, 1)], 10)                           # empty pool
     with pytest.raises(efg.EfannaError):
         idx.search_plan(16, (4, 10, 10, 20))                                         # k above pool
+
+
+def test_seeded_search_matches_oracle(efg, oracle_lib, setup):
+    """Entry seeds ahead of the tree leaves (ids >= n and repeats skipped) with per-query parameters."""
+    O = oracle_lib
+    idx, q, _, _ = setup
+    g = load_golden("mid_d128")
+    x = g["base"].astype(np.float32)
+    forest = O.Forest.load(os.path.join(GOLDEN, "mid_d128.trees"))
+    gp, gi = io.read_graph_csr(os.path.join(GOLDEN, "mid_d128.graph"))
+    rng = np.random.default_rng(5)
+    seeds = rng.integers(0, x.shape[0], (q.shape[0], 48)).astype(np.uint32)
+    seeds[:, 7] = seeds[:, 3]                  # a repeat
+    seeds[:, 11] = x.shape[0] + 5              # out of range
+    pick, params = _params(q.shape[0], 7)
+    params[:, 3] = np.minimum(params[:, 3], 10)
+    ref = O.search_batch(x, forest, gp, gi, q, params, 10, trees=8, seeds=seeds, threads=4)
+    Q = torch.from_numpy(q).cuda()
+    P = torch.from_numpy(params).cuda()
+    S = torch.from_numpy(seeds.view(np.int32)).cuda()
+    out = torch.zeros((q.shape[0], 10), dtype=torch.int32, device="cuda")
+    idx.knn_search_seeded_device(Q.data_ptr(), q.shape[0], q.shape[1], P.data_ptr(), (6, 1000, 150, 10),
+                                 S.data_ptr(), 48, out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    # pools made of seeds only (pool <= seeds per query)
+    small = np.tile(np.array([2, 30, 30, 10], np.int32), (q.shape[0], 1))
+    ref2 = O.search_batch(x, forest, gp, gi, q, small, 10, trees=8, seeds=seeds, threads=4)
+    P2 = torch.from_numpy(small).cuda()
+    idx.knn_search_seeded_device(Q.data_ptr(), q.shape[0], q.shape[1], P2.data_ptr(), (2, 30, 30, 10),
+                                 S.data_ptr(), 48, out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref2)

@@ -52,6 +52,21 @@ class QueryParams(C.Structure):
     _fields_ = [("epochs", C.c_int32), ("init_num", C.c_int32), ("extend_to", C.c_int32), ("k", C.c_uint32)]
 
 
+MAX_RUNGS = 16
+
+
+class LearnedParams(C.Structure):
+    _fields_ = [("clusters", C.c_uint32), ("kmeans_iters", C.c_uint32), ("kmeans_sample", C.c_uint32),
+                ("entries_per_cluster", C.c_uint32), ("entry_clusters", C.c_uint32), ("hidden", C.c_uint32),
+                ("rungs", C.c_uint32), ("rung", QueryParams * MAX_RUNGS), ("target", C.c_float),
+                ("train_epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64)]
+
+
+class LearnedStats(C.Structure):
+    _fields_ = [("train_queries", C.c_uint64), ("train_loss_first", C.c_float), ("train_loss_last", C.c_float),
+                ("rung_recall", C.c_float * MAX_RUNGS)]
+
+
 def query_params(rows) -> np.ndarray:
     """(epochs, pool, extend, k) rows -> a contiguous array laid out as efg_query_params."""
     a = np.ascontiguousarray(np.asarray(rows, dtype=np.int64).reshape(-1, 4).astype(np.int32))
@@ -137,6 +152,19 @@ def lib():
         "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_threads": (i32, [vp]),
         "efg_search_plan_destroy": (None, [vp]),
+        "efg_learned_default_params": (None, [C.POINTER(LearnedParams)]),
+        "efg_learned_create": (i32, [vp, C.POINTER(LearnedParams), C.POINTER(vp)]),
+        "efg_learned_train": (i32, [vp, vp, u64, u64]),
+        "efg_learned_predict_device": (i32, [vp, vp, u64, u64, vp, vp, vp]),
+        "efg_learned_search_device": (i32, [vp, vp, u64, u64, u32, i32, vp, vp]),
+        "efg_learned_get_stats": (i32, [vp, C.POINTER(LearnedStats)]),
+        "efg_learned_num_params": (u64, [vp]),
+        "efg_learned_get_weights": (i32, [vp, f32p]),
+        "efg_learned_set_weights": (i32, [vp, f32p]),
+        "efg_learned_get_norm": (i32, [vp, f32p, f32p]),
+        "efg_learned_grad": (i32, [vp, vp, u32, u64, vp, vp, C.POINTER(C.c_double), f32p]),
+        "efg_learned_clusters": (i32, [vp, vp, vp, vp]),
+        "efg_learned_destroy": (None, [vp]),
         "efg_nnd_init": (i32, [vp, C.POINTER(HostState)]),
         "efg_nnd_iterate": (i32, [vp, C.POINTER(HostState), u32, C.POINTER(C.c_uint64)]),
     }
@@ -340,6 +368,98 @@ class SearchPlan:
     def close(self):
         if self._h:
             lib().efg_search_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Learned:
+    """The learned form (efg_learned): k-means entry clusters + an MLP trained on search traces.
+    ``rungs`` is a list of (epochs, pool, extend) settings in ascending cost."""
+
+    def __init__(self, index: "Index", clusters=1024, entries_per_cluster=16, entry_clusters=8, hidden=256,
+                 rungs=None, target=0.9, train_epochs=8, batch=1024, lr=1e-3, kmeans_iters=10,
+                 kmeans_sample=100000, seed=1998):
+        p = LearnedParams()
+        lib().efg_learned_default_params(C.byref(p))
+        p.clusters, p.entries_per_cluster, p.entry_clusters, p.hidden = clusters, entries_per_cluster, \
+            entry_clusters, hidden
+        p.target, p.train_epochs, p.batch, p.lr = target, train_epochs, batch, lr
+        p.kmeans_iters, p.kmeans_sample, p.seed = kmeans_iters, kmeans_sample, seed
+        if rungs is not None:
+            p.rungs = len(rungs)
+            for i, r in enumerate(rungs):
+                p.rung[i] = QueryParams(int(r[0]), int(r[1]), int(r[2]), 10)
+        self.params = p
+        self.index = index
+        h = C.c_void_p()
+        _check(lib().efg_learned_create(index._h, C.byref(p), C.byref(h)))
+        self._h = h
+
+    @property
+    def rungs(self):
+        return [(self.params.rung[i].epochs, self.params.rung[i].init_num, self.params.rung[i].extend_to)
+                for i in range(self.params.rungs)]
+
+    def train_device(self, q_ptr: int, n: int, row_stride: int):
+        _check(lib().efg_learned_train(self._h, C.c_void_p(q_ptr), n, row_stride))
+
+    def predict_device(self, q_ptr: int, nq: int, row_stride: int, clusters_ptr: int, rung_ptr: int, stream: int = 0):
+        _check(lib().efg_learned_predict_device(self._h, C.c_void_p(q_ptr), nq, row_stride,
+                                                C.c_void_p(clusters_ptr or None), C.c_void_p(rung_ptr),
+                                                C.c_void_p(stream)))
+
+    def search_device(self, q_ptr: int, nq: int, row_stride: int, k: int, out_ptr: int, rung_bias: int = 0,
+                      stream: int = 0):
+        _check(lib().efg_learned_search_device(self._h, C.c_void_p(q_ptr), nq, row_stride, k, rung_bias,
+                                               C.c_void_p(out_ptr), C.c_void_p(stream)))
+
+    def stats(self) -> LearnedStats:
+        st = LearnedStats()
+        _check(lib().efg_learned_get_stats(self._h, C.byref(st)))
+        return st
+
+    def num_params(self) -> int:
+        return int(lib().efg_learned_num_params(self._h))
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros(self.num_params(), np.float32)
+        _check(lib().efg_learned_get_weights(self._h, _fp(w)))
+        return w
+
+    def set_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, np.float32)
+        _check(lib().efg_learned_set_weights(self._h, _fp(w)))
+
+    def norm(self):
+        d = self.index.dim
+        mean, istd = np.zeros(d, np.float32), np.zeros(d, np.float32)
+        _check(lib().efg_learned_get_norm(self._h, _fp(mean), _fp(istd)))
+        return mean, istd
+
+    def grad_device(self, x_ptr: int, B: int, row_stride: int, tc_ptr: int, tl_ptr: int):
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_double()
+        _check(lib().efg_learned_grad(self._h, C.c_void_p(x_ptr), B, row_stride, C.c_void_p(tc_ptr),
+                                      C.c_void_p(tl_ptr), C.byref(loss), _fp(g)))
+        return loss.value, g
+
+    def clusters(self):
+        n, C_, m = self.index.n, self.params.clusters, max(self.params.entries_per_cluster, 1)
+        a = np.zeros(n, np.int32)
+        e = np.zeros((C_, m), np.uint32)
+        c = np.zeros(C_, np.uint32)
+        _check(lib().efg_learned_clusters(self._h, C.c_void_p(a.ctypes.data), C.c_void_p(e.ctypes.data),
+                                          C.c_void_p(c.ctypes.data)))
+        return a, e, c
+
+    def close(self):
+        if self._h:
+            lib().efg_learned_destroy(self._h)
             self._h = None
 
     def __del__(self):

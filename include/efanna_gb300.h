@@ -156,6 +156,65 @@ int efg_knn_search_seeded_device(efg_index* idx, const float* d_queries, uint64_
                                  const uint32_t* d_seeds, uint32_t seeds_per_query, int32_t* d_out_ids,
                                  void* stream);
 
+/* Learned form (no reference counterpart).  A two-layer MLP (d -> hidden -> hidden -> clusters +
+ * rungs; BF16 weights and activations, FP32 accumulation; trained on the device by the library's own
+ * forward/backward/Adam kernels) predicts per query the k-means clusters of the base that hold its
+ * neighbours -- their `entries_per_cluster` members nearest the centroid become entry seeds of the
+ * pool -- and a search setting from the rung ladder (the early-stop pool size).  Training traces
+ * come from the method itself: exact neighbours of the training queries and the plain search's
+ * recall at every rung (label: the first rung reaching min(target, best recall)).  Plain search
+ * stays the fallback. */
+#define EFG_LEARNED_MAX_RUNGS 16
+typedef struct efg_learned_params {
+  uint32_t clusters;             /* k-means clusters of the base (entry-point classes)          */
+  uint32_t kmeans_iters;
+  uint32_t kmeans_sample;        /* base rows used by the k-means iterations                    */
+  uint32_t entries_per_cluster;  /* members nearest each centroid kept as seeds (0: no seeds)   */
+  uint32_t entry_clusters;       /* clusters predicted per query (<= 64; 0: no seeds)           */
+  uint32_t hidden;               /* hidden units per layer                                      */
+  uint32_t rungs;                /* settings in rung[], ascending cost                          */
+  efg_query_params rung[EFG_LEARNED_MAX_RUNGS];  /* k is ignored                              */
+  float target;                  /* per-query recall@10 that defines the rung label             */
+  uint32_t train_epochs;         /* passes over the traces                                      */
+  uint32_t batch;                /* training batch                                              */
+  float lr;                      /* Adam step                                                   */
+  uint64_t seed;
+} efg_learned_params;
+typedef struct efg_learned_stats {
+  uint64_t train_queries;
+  float train_loss_first, train_loss_last;       /* mean batch loss of the first and last pass  */
+  float rung_recall[EFG_LEARNED_MAX_RUNGS];      /* plain search's mean recall@10 per rung      */
+} efg_learned_stats;
+typedef struct efg_learned efg_learned;
+void efg_learned_default_params(efg_learned_params* p);
+/* Clusters the index's base (k-means on the device) and initialises the network. */
+int efg_learned_create(efg_index* idx, const efg_learned_params* params, efg_learned** out);
+/* Generates the traces for n training queries (device memory) and trains the network. */
+int efg_learned_train(efg_learned* lr, const float* d_queries, uint64_t n, uint64_t row_stride);
+/* Per query: entry_clusters predicted cluster ids (d_clusters, may be NULL when entry_clusters is 0)
+ * and the predicted rung (d_rung). */
+int efg_learned_predict_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                               uint32_t* d_clusters, uint32_t* d_rung, void* stream);
+/* Learned search: prediction, then the seeded nnexp search with each query at its predicted rung
+ * shifted by rung_bias (clamped to the ladder); nq rows of k ids into d_out. */
+int efg_learned_search_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                              uint32_t k, int rung_bias, int32_t* d_out, void* stream);
+int efg_learned_get_stats(const efg_learned* lr, efg_learned_stats* out);
+/* Network parameters as one FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (row-major, outputs x inputs). */
+uint64_t efg_learned_num_params(const efg_learned* lr);
+int efg_learned_get_weights(efg_learned* lr, float* host);
+int efg_learned_set_weights(efg_learned* lr, const float* host);
+/* Input standardisation (dim floats each): x' = (x - mean) * istd. */
+int efg_learned_get_norm(efg_learned* lr, float* mean, float* istd);
+/* Loss (mean over the batch) and its gradient for B query rows (device memory) with targets
+ * d_tclusters (B x 10 neighbour clusters) and d_tlabel (B rungs), without updating the network. */
+int efg_learned_grad(efg_learned* lr, const float* d_x, uint32_t B, uint64_t row_stride,
+                     const uint32_t* d_tclusters, const uint8_t* d_tlabel, double* loss, float* host_grad);
+/* Cluster of every base row (n int32), and per cluster its entry members (clusters x
+ * entries_per_cluster, 0xffffffff past the count) and counts; any pointer may be NULL. */
+int efg_learned_clusters(efg_learned* lr, int32_t* host_assign, uint32_t* host_entries, uint32_t* host_counts);
+void efg_learned_destroy(efg_learned* lr);
+
 /* A search plan: the batched nnexp launch sequence for up to `capacity` queries whose parameters
  * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers.  When
  * calibration queries are given (n_calib > 0, host memory, dim floats per row), the plan's

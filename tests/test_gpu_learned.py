@@ -1,0 +1,124 @@
+"""Learned form on the GPU: network gradients against the CPU oracle (oracle/mlp_oracle.py), the
+k-means entry lists, and training on the method's own traces -- what the trained network gains over
+the plain search it falls back to."""
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+from efanna_gb300 import datasets
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import mlp_oracle as M  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+RUNGS = [(2, 100, 20), (4, 300, 50), (6, 800, 100), (8, 1600, 200)]
+
+
+@pytest.fixture(scope="module")
+def small(efg):
+    x = datasets.mixture_u8(8000, 32, seed=21)
+    idx = efg.Index(x, efg.IndexParams(trees=8, merge_level=4, epochs=6))
+    idx.build_index()
+    idx.build_trees(8)
+    idx.set_search_params(4, 300, 50, 8)
+    yield idx, x
+    idx.close()
+
+
+def test_gradients_match_cpu_oracle(efg, small):
+    idx, x = small
+    L = efg.Learned(idx, clusters=16, entries_per_cluster=4, entry_clusters=2, hidden=48, rungs=RUNGS,
+                    kmeans_iters=4, kmeans_sample=4000)
+    rng = np.random.default_rng(3)
+    B = 96
+    q = datasets.mixture_u8(B, 32, seed=21, sample_seed=77)
+    tc = rng.integers(0, 16, (B, M.GT_K)).astype(np.uint32)
+    tl = rng.integers(0, len(RUNGS), B).astype(np.uint8)
+    w = L.weights() + rng.normal(0, 0.05, L.num_params()).astype(np.float32)  # away from the zero biases
+    L.set_weights(w)
+    mean, istd = L.norm()
+    Q = torch.from_numpy(q).cuda()
+    TC = torch.from_numpy(tc.view(np.int32)).cuda()
+    TL = torch.from_numpy(tl).cuda()
+    loss, g = L.grad_device(Q.data_ptr(), B, 32, TC.data_ptr(), TL.data_ptr())
+    rl, rg = M.loss_and_grad(w, q, mean, istd, tc.astype(np.int64), tl, 16, len(RUNGS), 48)
+    assert abs(loss - rl) / abs(rl) < 1e-4
+    assert np.linalg.norm(g - rg) / np.linalg.norm(rg) < 2e-3
+    # per block: no parameter group is off on its own
+    for part_g, part_r in zip(M.split(g, 32, 48, 16 + len(RUNGS)), M.split(rg, 32, 48, 16 + len(RUNGS))):
+        assert np.linalg.norm(part_g - part_r) <= 5e-3 * np.linalg.norm(part_r) + 1e-7
+    L.close()
+
+
+def test_clusters_and_entries(efg, small):
+    idx, x = small
+    L1 = efg.Learned(idx, clusters=32, entries_per_cluster=8, entry_clusters=4, hidden=32, rungs=RUNGS,
+                     kmeans_iters=5, kmeans_sample=6000)
+    a, e, c = L1.clusters()
+    assert a.min() >= 0 and a.max() < 32
+    sizes = np.bincount(a, minlength=32)
+    assert np.array_equal(c, np.minimum(sizes, 8))
+    for k in range(32):
+        ent = e[k, :c[k]]
+        assert np.all(a[ent] == k) and len(set(ent.tolist())) == len(ent)
+        assert np.all(e[k, c[k]:] == 0xFFFFFFFF)
+    L2 = efg.Learned(idx, clusters=32, entries_per_cluster=8, entry_clusters=4, hidden=32, rungs=RUNGS,
+                     kmeans_iters=5, kmeans_sample=6000)
+    a2, e2, _ = L2.clusters()
+    assert np.array_equal(a, a2) and np.array_equal(e, e2)  # deterministic
+    L1.close()
+    L2.close()
+
+
+def test_training_on_traces_and_learned_search(efg, small):
+    """Training lowers the loss; the learned search (predicted clusters as seeds, predicted rung)
+    is compared with the plain search at the same mean pool size (interpolated along the ladder)."""
+    idx, x = small
+    L = efg.Learned(idx, clusters=32, entries_per_cluster=8, entry_clusters=4, hidden=64, rungs=RUNGS,
+                    kmeans_iters=5, kmeans_sample=6000, train_epochs=30, batch=256, lr=2e-3, target=0.9)
+    tq = datasets.mixture_u8(6000, 32, seed=21, sample_seed=5)
+    TQ = torch.from_numpy(tq).cuda()
+    L.train_device(TQ.data_ptr(), tq.shape[0], 32)
+    st = L.stats()
+    assert st.train_queries == 6000 and st.train_loss_last < st.train_loss_first
+    rec = [st.rung_recall[i] for i in range(len(RUNGS))]
+    assert all(b >= a - 0.02 for a, b in zip(rec, rec[1:]))  # the ladder's recall grows with its cost
+    # held-out queries
+    q = datasets.mixture_u8(1000, 32, seed=21, queries=True)
+    Q = torch.from_numpy(q).cuda()
+    gt = torch.zeros((1000, 10), dtype=torch.int32, device="cuda")
+    X = torch.from_numpy(x).cuda()
+    efg.brute_force_knn_device(X.data_ptr(), x.shape[0], 32, 32, Q.data_ptr(), 1000, 32, 10, gt.data_ptr())
+    gtn = gt.cpu().numpy()
+
+    def recall(res):
+        return np.mean([len(set(a) & set(g)) / 10 for a, g in zip(res, gtn)])
+
+    # the plain search at every rung: its recall against the pool size
+    plain = []
+    for e, pool, ext in RUNGS:
+        idx.set_search_params(e, pool, ext, 8)
+        plain.append(recall(idx.knn_search(10, q)))
+    pools = [g[1] for g in RUNGS]
+    out = torch.zeros((1000, 10), dtype=torch.int32, device="cuda")
+    rung = torch.zeros(1000, dtype=torch.int32, device="cuda")
+    cl = torch.zeros((1000, 4), dtype=torch.int32, device="cuda")
+    L.predict_device(Q.data_ptr(), 1000, 32, cl.data_ptr(), rung.data_ptr())
+    torch.cuda.synchronize()
+    r = rung.cpu().numpy()
+    assert r.min() >= 0 and r.max() < len(RUNGS)
+    for bias in (0, 1):
+        L.search_device(Q.data_ptr(), 1000, 32, 10, out.data_ptr(), rung_bias=bias)
+        torch.cuda.synchronize()
+        res = out.cpu().numpy()
+        assert res.min() >= 0 and res.max() < x.shape[0]
+        mean_pool = np.mean([pools[min(i + bias, len(RUNGS) - 1)] for i in r])
+        at_cost = np.interp(mean_pool, pools, plain)  # the plain search at the same mean pool size
+        print("bias %d: learned recall %.4f at mean pool %.0f; plain recall at that pool %.4f (rungs %s)" %
+              (bias, recall(res), mean_pool, at_cost, ["%.4f" % v for v in plain]))
+        assert recall(res) >= at_cost - 0.01
+    L.close()

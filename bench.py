@@ -237,6 +237,7 @@ def run_gpu(args):
                 "overflow": int(st.overflow_queries), "reranked": int(st.reranked), "clocks": ck}
 
     runs = {p: measure(p) for p in ("fp32", "bf16")}
+    learned = None if args.no_learned else measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args)
     idx.set_search_precision("fp32")
     hbm, peak_kind = peaks()
 
@@ -283,6 +284,8 @@ def run_gpu(args):
         "gpu_launches": f32["launches"] * args.steps,
         "clocks": f32["clocks"],
     }
+    if learned is not None:
+        line["bf16_learned"] = learned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
     if rank == 0:
@@ -290,6 +293,73 @@ def run_gpu(args):
     idx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+LEARNED_RUNGS = [(4, 600, 60), (6, 1200, 120), (6, 2000, 200), (8, 3000, 300), (8, 4000, 400),
+                 (8, 6000, 600), (10, 9000, 900)]
+
+
+def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args):
+    """BF16 + learned: k-means entry clusters and an MLP trained on traces of held-out queries (their
+    own exact neighbours and the plain search's recall per rung), then the learned search with the
+    rung bias raised until recall@10 >= 0.95; device-timed like the plain arms."""
+    import torch
+    from efanna_gb300 import datasets
+    idx.set_search_precision("bf16")
+    t0 = time.perf_counter()
+    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=LEARNED_RUNGS,
+                  target=0.95, train_epochs=8, batch=1024, lr=1e-3)
+    torch.cuda.synchronize()
+    cluster_s = time.perf_counter() - t0
+    tq = datasets.mixture_u8(args.train_queries, 128, seed=0, sample_seed=4242)
+    TQ = torch.from_numpy(tq).cuda()
+    t0 = time.perf_counter()
+    L.train_device(TQ.data_ptr(), tq.shape[0], 128)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    st = L.stats()
+    out = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+    rung = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    clusters = torch.zeros((nq, 8), dtype=torch.int32, device="cuda")
+    L.predict_device(Q.data_ptr(), nq, 128, clusters.data_ptr(), rung.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    r = rung.cpu().numpy()
+    # early stop: the first rung whose predicted cumulative probability reaches the coverage
+    sweep, chosen = [], None
+    for cov in (0.5, 0.6, 0.7, 0.8, 0.85, 0.9, 0.95, 0.98, 0.995):
+        L.predict_device(Q.data_ptr(), nq, 128, clusters.data_ptr(), rung.data_ptr(), stream.cuda_stream, cov)
+        L.search_device(Q.data_ptr(), nq, 128, 10, out.data_ptr(), 0, stream.cuda_stream, cov)
+        torch.cuda.synchronize()
+        rc = recall(out.cpu().numpy(), gt)
+        pools = [LEARNED_RUNGS[i][1] for i in rung.cpu().numpy()]
+        sweep.append({"coverage": cov, "recall@10": round(rc, 4), "mean_pool": round(float(np.mean(pools)), 1)})
+        if rc >= TARGET:
+            chosen = cov
+            break
+    if chosen is None:
+        chosen = 0.995
+    for _ in range(args.warmup):
+        L.search_device(Q.data_ptr(), nq, 128, 10, out.data_ptr(), 0, stream.cuda_stream, chosen)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        L.search_device(Q.data_ptr(), nq, 128, 10, out.data_ptr(), 0, stream.cuda_stream, chosen)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    res = {"value": round(ws * nq * args.steps / (ms / 1e3), 1), "unit": "queries/s",
+           "ms_per_step": round(ms / args.steps, 4), "recall@10": sweep[-1]["recall@10"] if sweep else None,
+           "coverage": chosen, "sweep": sweep, "rungs": LEARNED_RUNGS,
+           "predicted_rung_histogram": np.bincount(r, minlength=len(LEARNED_RUNGS)).tolist(),
+           "train_queries": int(st.train_queries), "train_loss_first": round(st.train_loss_first, 4),
+           "train_loss_last": round(st.train_loss_last, 4),
+           "plain_rung_recall_train": [round(st.rung_recall[i], 4) for i in range(len(LEARNED_RUNGS))],
+           "cluster_s": round(cluster_s, 3), "trace_and_train_s": round(train_s, 3),
+           "form": "MLP (128-256-256-(1024 clusters + 7 rungs), BF16 weights, FP32 accumulate) picks 8 entry "
+                   "clusters (8 seeds each) and a rung per query; BF16 screening, FP32 re-rank"}
+    L.close()
+    return res
 
 
 def cpu_baseline(x, q, gt, point, idx, args):
@@ -375,6 +445,8 @@ def main():
     ap.add_argument("--cpu-queries", type=int, default=1000)
     ap.add_argument("--point", type=int, nargs=3, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

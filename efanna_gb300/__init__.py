@@ -155,8 +155,8 @@ def lib():
         "efg_learned_default_params": (None, [C.POINTER(LearnedParams)]),
         "efg_learned_create": (i32, [vp, C.POINTER(LearnedParams), C.POINTER(vp)]),
         "efg_learned_train": (i32, [vp, vp, u64, u64]),
-        "efg_learned_predict_device": (i32, [vp, vp, u64, u64, vp, vp, vp]),
-        "efg_learned_search_device": (i32, [vp, vp, u64, u64, u32, i32, vp, vp]),
+        "efg_learned_predict_device": (i32, [vp, vp, u64, u64, C.c_float, vp, vp, vp]),
+        "efg_learned_search_device": (i32, [vp, vp, u64, u64, u32, C.c_float, i32, vp, vp]),
         "efg_learned_get_stats": (i32, [vp, C.POINTER(LearnedStats)]),
         "efg_learned_num_params": (u64, [vp]),
         "efg_learned_get_weights": (i32, [vp, f32p]),
@@ -408,14 +408,15 @@ class Learned:
     def train_device(self, q_ptr: int, n: int, row_stride: int):
         _check(lib().efg_learned_train(self._h, C.c_void_p(q_ptr), n, row_stride))
 
-    def predict_device(self, q_ptr: int, nq: int, row_stride: int, clusters_ptr: int, rung_ptr: int, stream: int = 0):
-        _check(lib().efg_learned_predict_device(self._h, C.c_void_p(q_ptr), nq, row_stride,
+    def predict_device(self, q_ptr: int, nq: int, row_stride: int, clusters_ptr: int, rung_ptr: int, stream: int = 0,
+                       coverage: float = 0.0):
+        _check(lib().efg_learned_predict_device(self._h, C.c_void_p(q_ptr), nq, row_stride, coverage,
                                                 C.c_void_p(clusters_ptr or None), C.c_void_p(rung_ptr),
                                                 C.c_void_p(stream)))
 
     def search_device(self, q_ptr: int, nq: int, row_stride: int, k: int, out_ptr: int, rung_bias: int = 0,
-                      stream: int = 0):
-        _check(lib().efg_learned_search_device(self._h, C.c_void_p(q_ptr), nq, row_stride, k, rung_bias,
+                      stream: int = 0, coverage: float = 0.0):
+        _check(lib().efg_learned_search_device(self._h, C.c_void_p(q_ptr), nq, row_stride, k, coverage, rung_bias,
                                                C.c_void_p(out_ptr), C.c_void_p(stream)))
 
     def stats(self) -> LearnedStats:

@@ -348,9 +348,11 @@ __global__ void rung_label_kernel(const float* __restrict__ rec, uint64_t nq, ui
   label[q] = l;
 }
 
-// Per query (one warp): the E largest cluster logits (ties by index) and the argmax rung.
+// Per query (one warp): the E largest cluster logits (ties by index) and the rung: the argmax, or
+// with coverage > 0 the first rung whose cumulative softmax probability reaches it.
 __global__ void predict_kernel(const float* __restrict__ z, uint64_t nq, uint32_t O, uint32_t Cn, uint32_t R,
-                               uint32_t E, uint32_t* __restrict__ clusters, uint32_t* __restrict__ rung) {
+                               uint32_t E, float coverage, uint32_t* __restrict__ clusters,
+                               uint32_t* __restrict__ rung) {
   uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   uint32_t lane = threadIdx.x & 31;
   if (q >= nq) return;
@@ -383,6 +385,19 @@ __global__ void predict_kernel(const float* __restrict__ z, uint64_t nq, uint32_
     uint32_t br = 0;
     for (uint32_t r = 1; r < R; ++r)
       if (zr[Cn + r] > zr[Cn + br]) br = r;
+    if (coverage > 0.f) {
+      float mx = zr[Cn + br], se = 0.f;
+      for (uint32_t r = 0; r < R; ++r) se += expf(zr[Cn + r] - mx);
+      float cum = 0.f;
+      br = R - 1;
+      for (uint32_t r = 0; r < R; ++r) {
+        cum += expf(zr[Cn + r] - mx) / se;
+        if (cum >= coverage) {
+          br = r;
+          break;
+        }
+      }
+    }
     rung[q] = br;
   }
 }
@@ -737,7 +752,7 @@ int efg_learned_train(efg_learned* L, const float* d_q, uint64_t n, uint64_t row
 }
 
 int efg_learned_predict_device(efg_learned* L, const float* d_q, uint64_t nq, uint64_t row_stride,
-                               uint32_t* d_clusters, uint32_t* d_rung, void* stream) {
+                               float coverage, uint32_t* d_clusters, uint32_t* d_rung, void* stream) {
   if (!L || ((!d_q || !d_rung || (!d_clusters && L->p.entry_clusters)) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (row_stride < L->idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   cudaStream_t s = (cudaStream_t)stream;
@@ -749,7 +764,7 @@ int efg_learned_predict_device(efg_learned* L, const float* d_q, uint64_t nq, ui
                                          L->xb.p);
     forward(L, m, s);
     predict_kernel<<<(m * 32 + 255) / 256, 256, 0, s>>>(L->z.p, m, L->O, L->Cn, L->R, L->p.entry_clusters,
-                                                        d_clusters ? d_clusters + q0 * L->p.entry_clusters : nullptr,
+                                                        coverage, d_clusters ? d_clusters + q0 * L->p.entry_clusters : nullptr,
                                                         d_rung + q0);
     EFG_CUDA(cudaGetLastError());
   }
@@ -757,7 +772,7 @@ int efg_learned_predict_device(efg_learned* L, const float* d_q, uint64_t nq, ui
 }
 
 int efg_learned_search_device(efg_learned* L, const float* d_q, uint64_t nq, uint64_t row_stride, uint32_t k,
-                              int rung_bias, int32_t* d_out, void* stream) {
+                              float coverage, int rung_bias, int32_t* d_out, void* stream) {
   if (!L || ((!d_q || !d_out) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (nq == 0) return EFG_OK;
   efg_index* idx = L->idx;
@@ -774,7 +789,7 @@ int efg_learned_search_device(efg_learned* L, const float* d_q, uint64_t nq, uin
   EFG_TRY(L->pred_r.reserve(nq));
   EFG_TRY(L->seeds.reserve(std::max<uint64_t>(nq * E * m, 1)));
   EFG_TRY(L->qp.reserve(nq));
-  EFG_TRY(efg_learned_predict_device(L, d_q, nq, row_stride, E ? L->pred_c.p : nullptr, L->pred_r.p, s));
+  EFG_TRY(efg_learned_predict_device(L, d_q, nq, row_stride, coverage, E ? L->pred_c.p : nullptr, L->pred_r.p, s));
   assemble_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(L->pred_c.p, L->pred_r.p, nq, E, L->entries.p,
                                                               std::max<uint32_t>(m, 1), m, L->ladder.p, L->R,
                                                               rung_bias, k, L->seeds.p, L->qp.p);

@@ -192,13 +192,14 @@ int efg_learned_create(efg_index* idx, const efg_learned_params* params, efg_lea
 /* Generates the traces for n training queries (device memory) and trains the network. */
 int efg_learned_train(efg_learned* lr, const float* d_queries, uint64_t n, uint64_t row_stride);
 /* Per query: entry_clusters predicted cluster ids (d_clusters, may be NULL when entry_clusters is 0)
- * and the predicted rung (d_rung). */
+ * and the predicted rung (d_rung): the most likely rung, or with coverage > 0 the first rung whose
+ * cumulative predicted probability reaches coverage (the early stop). */
 int efg_learned_predict_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
-                               uint32_t* d_clusters, uint32_t* d_rung, void* stream);
+                               float coverage, uint32_t* d_clusters, uint32_t* d_rung, void* stream);
 /* Learned search: prediction, then the seeded nnexp search with each query at its predicted rung
  * shifted by rung_bias (clamped to the ladder); nq rows of k ids into d_out. */
 int efg_learned_search_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
-                              uint32_t k, int rung_bias, int32_t* d_out, void* stream);
+                              uint32_t k, float coverage, int rung_bias, int32_t* d_out, void* stream);
 int efg_learned_get_stats(const efg_learned* lr, efg_learned_stats* out);
 /* Network parameters as one FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (row-major, outputs x inputs). */
 uint64_t efg_learned_num_params(const efg_learned* lr);

@@ -111,14 +111,18 @@ def test_training_on_traces_and_learned_search(efg, small):
     torch.cuda.synchronize()
     r = rung.cpu().numpy()
     assert r.min() >= 0 and r.max() < len(RUNGS)
-    for bias in (0, 1):
-        L.search_device(Q.data_ptr(), 1000, 32, 10, out.data_ptr(), rung_bias=bias)
+    for bias, cov in ((0, 0.0), (1, 0.0), (0, 0.9)):
+        L.search_device(Q.data_ptr(), 1000, 32, 10, out.data_ptr(), rung_bias=bias, coverage=cov)
         torch.cuda.synchronize()
         res = out.cpu().numpy()
         assert res.min() >= 0 and res.max() < x.shape[0]
+        if cov > 0:  # the rungs chosen by cumulative probability
+            L.predict_device(Q.data_ptr(), 1000, 32, cl.data_ptr(), rung.data_ptr(), coverage=cov)
+            torch.cuda.synchronize()
+            r = rung.cpu().numpy()
         mean_pool = np.mean([pools[min(i + bias, len(RUNGS) - 1)] for i in r])
         at_cost = np.interp(mean_pool, pools, plain)  # the plain search at the same mean pool size
-        print("bias %d: learned recall %.4f at mean pool %.0f; plain recall at that pool %.4f (rungs %s)" %
-              (bias, recall(res), mean_pool, at_cost, ["%.4f" % v for v in plain]))
+        print("bias %d coverage %.2f: learned recall %.4f at mean pool %.0f; plain recall at that pool %.4f "
+              "(rungs %s)" % (bias, cov, recall(res), mean_pool, at_cost, ["%.4f" % v for v in plain]))
         assert recall(res) >= at_cost - 0.01
     L.close()

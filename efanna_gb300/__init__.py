@@ -129,6 +129,7 @@ def lib():
         "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
         "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
         "efg_set_search_precision": (i32, [vp, i32]),
+        "efg_screen_distances": (i32, [vp, i32, vp, u64, u64, vp, u32, vp, vp]),
         "efg_knn_search": (i32, [vp, f32p, u64, u32, u64, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_device": (i32, [vp, vp, u64, u64, u32, vp, vp]),
         "efg_get_search_stats": (i32, [vp, C.POINTER(SearchStats)]),
@@ -245,11 +246,17 @@ class Index:
                                            search_method))
 
     def set_search_precision(self, precision: str) -> None:
-        """'fp32' (the reference's arithmetic) or 'bf16' (BF16 screening, FP32 re-rank)."""
-        code = {"fp32": 0, "bf16": 1}.get(precision)
+        """'fp32' (the reference's arithmetic), 'bf16' or 'fp8' (screening in that format, FP32 re-rank)."""
+        code = {"fp32": 0, "bf16": 1, "fp8": 2}.get(precision)
         if code is None:
-            raise ValueError("precision must be 'fp32' or 'bf16'")
+            raise ValueError("precision must be 'fp32', 'bf16' or 'fp8'")
         _check(lib().efg_set_search_precision(self._h, code))
+
+    def screen_distances_device(self, precision: str, q_ptr: int, nq: int, row_stride: int, ids_ptr: int, m: int,
+                                out_ptr: int, stream: int = 0):
+        code = {"fp32": 0, "bf16": 1, "fp8": 2}[precision]
+        _check(lib().efg_screen_distances(self._h, code, C.c_void_p(q_ptr), nq, row_stride, C.c_void_p(ids_ptr), m,
+                                          C.c_void_p(out_ptr), C.c_void_p(stream)))
 
     def knn_search(self, k: int, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, dtype=np.float32)

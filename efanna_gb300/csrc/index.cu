@@ -305,6 +305,8 @@ void efg_index_destroy(efg_index* idx) {
   idx->ht_scratch.release();
   idx->ovf_list.release();
   idx->base16.release();
+  idx->base8.release();
+  idx->scale8.release();
   idx->kg_keys.release();
   idx->qp_buf.release();
   idx->kg_bits.release();
@@ -358,11 +360,19 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
 
 int efg_set_search_precision(efg_index* idx, int precision) {
   if (!idx) return fail(EFG_ERR_ARG, "null index");
-  if (precision != EFG_PRECISION_FP32 && precision != EFG_PRECISION_BF16)
-    return fail(EFG_ERR_ARG, "precision must be EFG_PRECISION_FP32 or EFG_PRECISION_BF16");
+  if (precision != EFG_PRECISION_FP32 && precision != EFG_PRECISION_BF16 && precision != EFG_PRECISION_FP8)
+    return fail(EFG_ERR_ARG, "precision must be EFG_PRECISION_FP32, EFG_PRECISION_BF16 or EFG_PRECISION_FP8");
   if (precision == EFG_PRECISION_BF16 && !idx->base16.p) EFG_TRY(make_base16(idx));
+  if (precision == EFG_PRECISION_FP8 && !idx->base8.p) EFG_TRY(make_base8(idx));
   idx->precision = precision;
   return EFG_OK;
+}
+
+int efg_screen_distances(efg_index* idx, int precision, const float* d_q, uint64_t nq, uint64_t row_stride,
+                         const uint32_t* d_ids, uint32_t m, float* d_out, void* stream) {
+  if (!idx || ((!d_q || !d_ids || !d_out) && nq && m)) return fail(EFG_ERR_ARG, "null argument");
+  if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
+  return screen_pairs(idx, precision, d_q, nq, row_stride, d_ids, m, d_out, (cudaStream_t)stream);
 }
 
 int efg_knn_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t row_stride, uint32_t k,

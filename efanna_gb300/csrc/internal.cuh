@@ -105,6 +105,9 @@ struct efg_index {
   int precision = 0;
   efg::DevBuf<uint16_t> base16;
   uint32_t ld16 = 0;
+  efg::DevBuf<uint8_t> base8;   // FP8 e4m3 screening copy (ld8 bytes per row) and per-row scales
+  efg::DevBuf<float> scale8;
+  uint32_t ld8 = 0;
   // kgraph search scratch: pool keys per query, visited bitsets per warp
   efg::DevBuf<uint64_t> kg_keys;
   efg::DevBuf<uint32_t> kg_bits;
@@ -139,6 +142,11 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
                      bool count_evals, const uint32_t* d_seeds = nullptr, uint32_t seeds_per_query = 0);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
+// Builds the FP8 e4m3 screening copy of the base with one FP32 scale per row.
+int make_base8(efg_index* idx);
+// Screening distances of (query, id) pairs in a given precision (the search's gather).
+int screen_pairs(efg_index* idx, int precision, const float* d_q, uint64_t nq, uint64_t qld, const uint32_t* d_ids,
+                 uint32_t m, float* d_out, cudaStream_t s);
 // kgraph.cu: search method 1 (getNeighbors_kgraph).
 int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                          cudaStream_t s, bool count_evals);

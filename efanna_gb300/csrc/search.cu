@@ -29,6 +29,8 @@
 #include <algorithm>
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include "search.cuh"
 
@@ -137,6 +139,34 @@ __global__ void to_bf16_kernel(const float* __restrict__ base, uint64_t n, uint3
   }
 }
 
+// FP8 e4m3 rows with one scale per row: scale = max|x| / 448 (the largest e4m3 value), values
+// x / scale rounded to nearest (saturating), rows padded with zeros to ld8 bytes.  One warp per row.
+__global__ void to_fp8_kernel(const float* __restrict__ base, uint64_t n, uint32_t dim, uint32_t ld,
+                              uint8_t* __restrict__ out, uint32_t ld8, float* __restrict__ scale) {
+  uint64_t r = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint32_t lane = threadIdx.x & 31;
+  if (r >= n) return;
+  const float* row = base + r * ld;
+  float mx = 0.f;
+  for (uint32_t j = lane; j < dim; j += 32) mx = fmaxf(mx, fabsf(row[j]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  float s = mx > 0.f ? mx / 448.f : 1.f;
+  for (uint32_t j = lane; j < ld8; j += 32)
+    out[r * ld8 + j] = j < dim ? (uint8_t)__nv_cvt_float_to_fp8(row[j] / s, __NV_SATFINITE, __NV_E4M3) : 0;
+  if (lane == 0) scale[r] = s;
+}
+
+int make_base8(efg_index* idx) {
+  idx->ld8 = (uint32_t)round_up(idx->dim, 16);
+  EFG_TRY(idx->base8.reserve(idx->n * idx->ld8));
+  EFG_TRY(idx->scale8.reserve(idx->n));
+  to_fp8_kernel<<<(unsigned)((idx->n * 32 + 255) / 256), 256, 0, idx->stream>>>(idx->d_base, idx->n, idx->dim, idx->ld,
+                                                                                idx->base8.p, idx->ld8, idx->scale8.p);
+  EFG_CUDA(cudaGetLastError());
+  EFG_CUDA(cudaStreamSynchronize(idx->stream));
+  return EFG_OK;
+}
+
 int make_base16(efg_index* idx) {
   idx->ld16 = (uint32_t)round_up(idx->dim, 8);
   EFG_TRY(idx->base16.reserve(idx->n * idx->ld16));
@@ -169,6 +199,43 @@ int launch_row_sort(uint64_t* keys, uint64_t nq, uint32_t stride, uint32_t count
   for (uint64_t q0 = 0; q0 < nq; q0 += 65535) {
     uint64_t m = std::min<uint64_t>(nq - q0, 65535);
     row_sort_kernel<<<(unsigned)m, 512, smem, s>>>(keys + q0 * stride, stride, count, p2);
+    EFG_CUDA(cudaGetLastError());
+  }
+  return EFG_OK;
+}
+
+int screen_pairs(efg_index* idx, int precision, const float* d_q, uint64_t nq, uint64_t qld, const uint32_t* d_ids,
+                 uint32_t m, float* d_out, cudaStream_t s) {
+  if (m == 0 || nq == 0) return EFG_OK;
+  if (m > 4096) return fail(EFG_ERR_ARG, "at most 4096 ids per query");
+  SearchCfg cfg{};
+  if (precision == EFG_PRECISION_FP8) {
+    if (!idx->base8.p) EFG_TRY(make_base8(idx));
+    cfg.fp8 = 1;
+    cfg.screened = 1;
+    cfg.ld8 = idx->ld8;
+    cfg.cpr8 = idx->ld8 / 16;
+    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr8), 32);
+    while ((1u << cfg.gshift8) < g) ++cfg.gshift8;
+  } else if (precision == EFG_PRECISION_BF16) {
+    if (!idx->base16.p) EFG_TRY(make_base16(idx));
+    cfg.screened = 1;
+    cfg.ld16 = idx->ld16;
+    cfg.cpr16 = idx->ld16 / 8;
+    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr16), 32);
+    while ((1u << cfg.gshift16) < g) ++cfg.gshift16;
+  } else if (precision != EFG_PRECISION_FP32) {
+    return fail(EFG_ERR_ARG, "unknown precision");
+  }
+  cfg.q4 = std::max<uint32_t>(std::max<uint32_t>(idx->ld / 4, cfg.screened && !cfg.fp8 ? cfg.ld16 / 4 : 0u),
+                              cfg.fp8 ? cfg.ld8 / 4 : 0u);
+  size_t smem = round_up((size_t)cfg.q4 * 16 + (size_t)m * 4, 16) + (size_t)m * 8;
+  EFG_CUDA(cudaFuncSetAttribute(s256::screen_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for (uint64_t q0 = 0; q0 < nq; q0 += 65535) {
+    uint64_t b = std::min<uint64_t>(nq - q0, 65535);
+    s256::screen_pairs_kernel<<<(unsigned)b, 256, smem, s>>>(idx->d_base, idx->dim, idx->ld, idx->base16.p,
+                                                             idx->base8.p, idx->scale8.p, cfg, d_q + q0 * qld, qld,
+                                                             d_ids + q0 * m, m, d_out + q0 * m);
     EFG_CUDA(cudaGetLastError());
   }
   return EFG_OK;
@@ -259,14 +326,15 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
       idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.cnl.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
       idx->graph.ids.p, d_q, nq, qld, c1, d_out, idx->eval_counter.p, idx->ht_scratch.p, nullptr,
-      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys, d_params, d_nq, d_seeds);
+      two_pass ? idx->ovf_list.p : nullptr, idx->base16.p, d_keys, d_params, d_nq, d_seeds, idx->base8.p,
+      idx->scale8.p);
   cudaError_t le = cudaGetLastError();
   *launches = 1;
   if (le == cudaSuccess && two_pass) {
     kernel<<<(unsigned)grid2, threads, smem2, s>>>(
         idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.cnl.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
         idx->graph.ids.p, d_q, nq, qld, c2, d_out, idx->eval_counter.p, idx->ht_scratch.p, idx->ovf_list.p, nullptr,
-        idx->base16.p, d_keys, d_params, d_nq, d_seeds);
+        idx->base16.p, d_keys, d_params, d_nq, d_seeds, idx->base8.p, idx->scale8.p);
     le = cudaGetLastError();
     *launches = 2;
   }
@@ -330,9 +398,17 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
   cfg.nseeds = d_seeds ? seeds_per_query : 0;
-  if (idx->precision == EFG_PRECISION_BF16) {
-    if (!idx->base16.p) EFG_TRY(make_base16(idx));
-    cfg.bf16 = 1;
+  if (idx->precision == EFG_PRECISION_FP8) {
+    if (!idx->base8.p) EFG_TRY(make_base8(idx));
+    cfg.fp8 = 1;
+    cfg.ld8 = idx->ld8;
+    cfg.cpr8 = idx->ld8 / 16;
+    uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr8), 32);
+    while ((1u << cfg.gshift8) < g) ++cfg.gshift8;
+  }
+  if (idx->precision == EFG_PRECISION_BF16 || idx->precision == EFG_PRECISION_FP8) {
+    if (idx->precision == EFG_PRECISION_BF16 && !idx->base16.p) EFG_TRY(make_base16(idx));
+    cfg.screened = 1;
     cfg.ld16 = idx->ld16;
     cfg.cpr16 = idx->ld16 / 8;
     uint32_t g = std::min<uint32_t>(next_pow2(cfg.cpr16), 32);
@@ -353,7 +429,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
                         cfg.nseeds ? d_seeds : nullptr);
   cudaEventRecord(e1, s);
   if (rc == EFG_OK && count_evals)
-    rc = finish_search_stats(idx, s, e0, e1, nq, launches == 2, launches, cfg.bf16 ? cfg.rerank : 0);
+    rc = finish_search_stats(idx, s, e0, e1, nq, launches == 2, launches, cfg.screened ? cfg.rerank : 0);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;

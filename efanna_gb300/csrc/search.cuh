@@ -20,9 +20,13 @@ struct SearchCfg {
   uint32_t o_lstart, o_seqoff, o_tkey, o_tpos;  // fill phase (absolute)
   uint32_t o_res, o_tmp, o_newk, o_surv;                // select phase (absolute)
   uint32_t q4;          // staged query length in float4 (covers both row layouts)
-  // BF16 screening: rows ld16 values apart, cpr16 16-byte chunks per row, 2^gshift16 lanes per
-  // row in the gather; the first `rerank` results are re-scored in FP32 before the k are emitted
-  uint32_t bf16, ld16, cpr16, gshift16, rerank;
+  // reduced-precision screening (BF16 or FP8): BF16 rows ld16 values apart, cpr16 16-byte chunks
+  // per row, 2^gshift16 lanes per row in the gather; the first `rerank` results are re-scored in
+  // FP32 before the k are emitted
+  uint32_t screened, ld16, cpr16, gshift16, rerank;
+  // FP8 (e4m3, one FP32 scale per row) screening instead of BF16: rows ld8 bytes apart, cpr8
+  // 16-byte chunks per row, 2^gshift8 lanes per row
+  uint32_t fp8, ld8, cpr8, gshift8;
   uint32_t emit_pool;   // stop after the pool and write its keys (kgraph's first stage)
   uint32_t fixed_k;     // graph degree when every row has it (0: row pointers), and
   uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices

@@ -113,7 +113,13 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
  * best of those.  Ids can differ from the FP32 search where BF16 rounding reorders candidates. */
 #define EFG_PRECISION_FP32 0
 #define EFG_PRECISION_BF16 1
+#define EFG_PRECISION_FP8 2  /* e4m3 copy with one FP32 scale per row (max|x| / 448); same re-rank */
 int efg_set_search_precision(efg_index* idx, int precision);
+/* The search's screening distances for given pairs: query q (device memory, row_stride floats apart)
+ * against ids d_ids[q*m .. q*m + m) (m <= 4096), in `precision`; FP32 results into d_out (nq x m).
+ * Used to state each precision's distance error against an FP64 reference. */
+int efg_screen_distances(efg_index* idx, int precision, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                         const uint32_t* d_ids, uint32_t m, float* d_out, void* stream);
 
 /* FIndex::knnSearch — efanna.hpp:32-34, base_index.hpp:311-313.  Host queries in, host ids out
  * (nq*k int32).  The ids are also kept for efg_save_results. */

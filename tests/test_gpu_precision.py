@@ -6,6 +6,7 @@ the FP32 walk and the ids must be identical.  On real-valued data the ids may di
 rounding reorders near-ties; recall against exact neighbours must stay within 0.01 of FP32's.
 """
 import numpy as np
+import torch
 import pytest
 
 from efanna_gb300 import datasets
@@ -97,6 +98,64 @@ def test_precision_argument_errors(efg):
     x = datasets.mixture_u8(3000, 16, seed=7).astype(np.float32)
     idx = efg.Index(x, efg.IndexParams())
     with pytest.raises(ValueError):
-        idx.set_search_precision("fp8")
+        idx.set_search_precision("fp4")
     with pytest.raises(efg.EfannaError):
         efg._check(efg.lib().efg_set_search_precision(idx._h, 7))
+
+
+def _rel_errors(efg, idx, x, q, precision, m=256, seed=0):
+    rng = np.random.default_rng(seed)
+    ids = rng.integers(0, x.shape[0], (q.shape[0], m)).astype(np.uint32)
+    Q = torch.from_numpy(np.ascontiguousarray(q, np.float32)).cuda()
+    I = torch.from_numpy(ids.view(np.int32)).cuda()
+    out = torch.zeros((q.shape[0], m), dtype=torch.float32, device="cuda")
+    idx.screen_distances_device(precision, Q.data_ptr(), q.shape[0], q.shape[1], I.data_ptr(), m, out.data_ptr())
+    torch.cuda.synchronize()
+    d = out.cpu().numpy().astype(np.float64)
+    x64, q64 = x.astype(np.float64), q.astype(np.float64)
+    ref = ((x64[ids] - q64[:, None, :]) ** 2).sum(-1)
+    rel = np.abs(d - ref) / np.maximum(ref, 1e-30)
+    return rel.max(), rel.mean()
+
+
+def test_distance_error_against_fp64(efg):
+    """Each screening precision's squared-distance error against FP64: the unit-block GIST-like
+    data (d = 960, values in [0, 1]) and the byte-valued data (d = 128)."""
+    xu = datasets.mixture_unit(20000, 960, seed=9)
+    qu = datasets.mixture_unit(64, 960, seed=9, queries=True)
+    iu = efg.Index(xu, efg.IndexParams())
+    e32 = _rel_errors(efg, iu, xu, qu, "fp32")
+    e16 = _rel_errors(efg, iu, xu, qu, "bf16")
+    e8 = _rel_errors(efg, iu, xu, qu, "fp8")
+    print("d=960 unit data: relative error max/mean fp32 %.2e/%.2e bf16 %.2e/%.2e fp8 %.2e/%.2e" %
+          (e32 + e16 + e8))
+    assert e32[0] < 1e-5
+    assert e16[1] < 5e-3 and e16[0] < 5e-2
+    assert e8[1] < 5e-2 and e8[0] < 3e-1
+    xb = datasets.mixture_u8(20000, 128, seed=9)
+    qb = datasets.mixture_u8(64, 128, seed=9, queries=True)
+    ib = efg.Index(xb, efg.IndexParams())
+    assert _rel_errors(efg, ib, xb, qb, "fp32")[0] == 0.0  # integers: exact in any order
+    assert _rel_errors(efg, ib, xb, qb, "bf16")[0] == 0.0  # bytes are exact in BF16
+    e8b = _rel_errors(efg, ib, xb, qb, "fp8")
+    print("d=128 byte data: fp8 relative error max/mean %.2e/%.2e" % e8b)
+    assert 0 < e8b[1] < 5e-2
+
+
+def test_screened_search_recall_at_100(efg):
+    """The high-dimensional precision workload at small scale: d = 960 unit-block data, a K = 100
+    graph (L = 200, check = 200), recall@100 of FP32, BF16 and FP8 screening with the FP32 re-rank."""
+    x = datasets.mixture_unit(20000, 960, seed=13)
+    q = datasets.mixture_unit(200, 960, seed=13, queries=True)
+    gt = _exact_knn(x, q, 100)
+    idx = efg.Index(x, efg.IndexParams(trees=8, merge_level=8, epochs=8, check=200, L=200, K=100, S=10))
+    idx.build_index()
+    idx.set_search_params(4, 1200, 200, 8)
+    rec = {}
+    for prec in ("fp32", "bf16", "fp8"):
+        idx.set_search_precision(prec)
+        res = idx.knn_search(100, q)
+        rec[prec] = np.mean([len(set(r) & set(g)) / 100 for r, g in zip(res, gt)])
+    print("recall@100: fp32 %.4f bf16 %.4f fp8 %.4f" % (rec["fp32"], rec["bf16"], rec["fp8"]))
+    assert rec["bf16"] >= rec["fp32"] - 0.01
+    assert rec["fp8"] >= rec["fp32"] - 0.03

@@ -196,9 +196,9 @@ def run_gpu(args):
         st = idx.search_stats()
         evals_q = st.distance_evals / nq
         exp_q = st.expanded_nodes / nq
-        row_bytes = 128 * (2 if precision == "bf16" else 4)
+        row_bytes = {"fp32": 128 * 4, "bf16": 128 * 2, "fp8": 128 + 4}[precision]  # fp8: bytes + row scale
         # algorithmic bytes per query: screened rows + graph rows of expanded nodes + leaf ids + query
-        # (+ the FP32 rows re-ranked after BF16 screening)
+        # (+ the FP32 rows re-ranked after BF16/FP8 screening)
         bytes_q = evals_q * row_bytes + exp_q * GRAPH["K"] * 4 + point[1] * 4 + 128 * 4 + st.reranked * 128 * 4
         for _ in range(args.warmup):
             search_once(point)
@@ -236,7 +236,7 @@ def run_gpu(args):
                 "evals_q": evals_q, "exp_q": exp_q, "bytes_q": bytes_q, "launches": int(st.kernel_launches),
                 "overflow": int(st.overflow_queries), "reranked": int(st.reranked), "clocks": ck}
 
-    runs = {p: measure(p) for p in ("fp32", "bf16")}
+    runs = {p: measure(p) for p in ("fp32", "bf16", "fp8")}
     learned = None if args.no_learned else measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args)
     idx.set_search_precision("fp32")
     hbm, peak_kind = peaks()
@@ -255,6 +255,13 @@ def run_gpu(args):
         return {"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(r["recall"], 4)}
 
     f32, b16 = runs["fp32"], runs["bf16"]
+
+    def screened(r, form):
+        return {"value": round(r["value"], 1), "unit": "queries/s", "ms_per_step": round(r["per_step_ms"], 4),
+                "e2e": round(r["e2e"], 1), "operating_point": point_of(r), "ladder": r["ladder"],
+                "config_point_recall@10": round(r["config_recall"], 4), "reranked_per_query": r["reranked"],
+                "roofline": roofline(r), "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"],
+                "form": form}
     line = {
         "metric": METRIC, "value": round(f32["value"], 1), "unit": "queries/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(f32["per_step_ms"], 4),
@@ -275,12 +282,9 @@ def run_gpu(args):
         "e2e": {"value": round(f32["e2e"], 1), "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(nq * 10 * 4)},
         "roofline": roofline(f32),
-        "bf16": {"value": round(b16["value"], 1), "unit": "queries/s", "ms_per_step": round(b16["per_step_ms"], 4),
-                 "e2e": round(b16["e2e"], 1), "operating_point": point_of(b16), "ladder": b16["ladder"],
-                 "config_point_recall@10": round(b16["config_recall"], 4), "reranked_per_query": b16["reranked"],
-                 "roofline": roofline(b16), "gpu_launches": b16["launches"] * args.steps,
-                 "clocks": b16["clocks"],
-                 "form": "BF16 copy of the base screens the walk, the best max(2k, k+32) re-ranked in FP32"},
+        "bf16": screened(b16, "BF16 copy of the base screens the walk, the best max(2k, k+32) re-ranked in FP32"),
+        "fp8": screened(runs["fp8"], "FP8 e4m3 copy (one FP32 scale per row) screens the walk, the best "
+                                     "max(2k, k+32) re-ranked in FP32"),
         "gpu_launches": f32["launches"] * args.steps,
         "clocks": f32["clocks"],
     }

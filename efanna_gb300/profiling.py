@@ -77,7 +77,7 @@ if __name__ == "__main__":
     s.add_argument("--trees", type=int, default=16)
     s.add_argument("--also", type=int, nargs=3, action="append", default=[],
                    help="further epochs/pool/extend points to time after --point")
-    s.add_argument("--precision", nargs="+", default=["fp32"], choices=["fp32", "bf16"])
+    s.add_argument("--precision", nargs="+", default=["fp32"], choices=["fp32", "bf16", "fp8"])
     s.add_argument("--repeat", type=int, default=2)
     a = ap.parse_args()
     if a.cmd == "table":

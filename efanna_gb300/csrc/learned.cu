@@ -33,7 +33,6 @@ namespace {
 constexpr uint32_t FULLMASK = 0xffffffffu;
 constexpr int GT_K = 10;  // neighbours per training query in the traces
 
-__device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
 __device__ __forceinline__ float ld_as_float(const float* p) { return *p; }
 __device__ __forceinline__ float ld_as_float(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 

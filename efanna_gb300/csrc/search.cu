@@ -50,7 +50,8 @@ enum : uint32_t { SERR_FRONTIER = 1u, SERR_HASH = 2u };
 __device__ __forceinline__ uint32_t ht_slot(uint32_t id, uint32_t size) { return __umulhi(id * 2654435761u, size); }
 
 // Inserts id into the visited set; true if it was not present.  When the set already holds
-// `limit` ids the insert is refused and *ovf is set (the query goes to the overflow pass).
+// `limit` ids (*count, which callers advance by the inserts they made, a warp at a time) the insert
+// is refused and *ovf is set (the query goes to the overflow pass).
 __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t size, uint32_t limit, uint32_t* count,
                                           uint32_t* ovf, uint32_t id) {
   uint32_t h = ht_slot(id, size);
@@ -62,10 +63,7 @@ __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t size, uint32_t 
         return false;
       }
       uint32_t prev = atomicCAS(&ht[h], kEmpty, id);
-      if (prev == kEmpty) {
-        atomicAdd(count, 1u);
-        return true;
-      }
+      if (prev == kEmpty) return true;
       cur = prev;
     }
     if ((cur & ID_MASK) == id) return false;

@@ -22,10 +22,11 @@
 // into it 1024 at a time: keys at or above the current worst are dropped, the rest sorted and
 // merged by rank.  Ids are unique, so the result does not depend on the order threads find them.
 //
-// The visited set (the reference's N-bit tbflag, with bit 31 of a slot as the "expanded" mark,
-// the reference's newflag) is an open-addressing table in shared memory sized for the expected
-// number of visits.  A query that fills it past its limit is abandoned and listed; a second
-// launch answers the listed queries with a worst-case-sized table in global memory.
+// The visited set (the reference's N-bit tbflag) is a double-hashing table in shared memory sized
+// for the expected number of visits; the reference's newflag ("expanded") is a bit of the result
+// keys.  A query whose set reaches 80% of the table at a phase boundary moves it to a worst-case
+// table in global scratch; one that fills 90% within a phase is abandoned and listed, and a second
+// launch answers the listed queries with worst-case tables in global memory.
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -42,19 +43,30 @@ static constexpr int FILL_CHUNK = 1024;  // sequence positions deduplicated per 
 static constexpr int FILL_TAB = 2048;    // chunk-local id table
 static constexpr int SEL_CHUNK = 1024;   // candidates folded into the result list per step
 static constexpr uint32_t ID_MASK = 0x3FFFFFFFu;
-static constexpr uint32_t EXPANDED = 0x80000000u;
 
 enum : uint32_t { SERR_FRONTIER = 1u, SERR_HASH = 2u };
 
 
 __device__ __forceinline__ uint32_t ht_slot(uint32_t id, uint32_t size) { return __umulhi(id * 2654435761u, size); }
+// Double hashing: a second, odd probe step that is not a multiple of 3 -- coprime with every table
+// size used here (2^k or 3 * 2^k slots), so a probe sequence visits every slot; it avoids the
+// long clustered runs of linear probing at high load.
+__device__ __forceinline__ uint32_t ht_step(uint32_t id, uint32_t size) {
+  uint32_t st = 2 * __umulhi((id ^ (id >> 15)) * 0x85EBCA6Bu, size >> 1) + 1;
+  if (st % 3 == 0) st = st + 2 < size ? st + 2 : st - 2;
+  return st;
+}
+__device__ __forceinline__ uint32_t ht_next(uint32_t h, uint32_t st, uint32_t size) {
+  h += st;
+  return h >= size ? h - size : h;
+}
 
 // Inserts id into the visited set; true if it was not present.  When the set already holds
 // `limit` ids (*count, which callers advance by the inserts they made, a warp at a time) the insert
 // is refused and *ovf is set (the query goes to the overflow pass).
 __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t size, uint32_t limit, uint32_t* count,
                                           uint32_t* ovf, uint32_t id) {
-  uint32_t h = ht_slot(id, size);
+  uint32_t h = ht_slot(id, size), st = ht_step(id, size);
   for (uint32_t probe = 0; probe < size; ++probe) {
     uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
     if (cur == kEmpty) {
@@ -67,29 +79,18 @@ __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t size, uint32_t 
       cur = prev;
     }
     if ((cur & ID_MASK) == id) return false;
-    if (++h == size) h = 0;
+    h = ht_next(h, st, size);
   }
   atomicOr(ovf, 1u);
   return false;
 }
 __device__ __forceinline__ bool ht_contains(const uint32_t* ht, uint32_t size, uint32_t id) {
-  uint32_t h = ht_slot(id, size);
+  uint32_t h = ht_slot(id, size), st = ht_step(id, size);
   for (uint32_t probe = 0; probe < size; ++probe) {
     uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
     if (cur == kEmpty) return false;
     if ((cur & ID_MASK) == id) return true;
-    if (++h == size) h = 0;
-  }
-  return false;
-}
-// Marks id expanded; true if this call did it.
-__device__ __forceinline__ bool ht_mark_expanded(uint32_t* ht, uint32_t size, uint32_t id) {
-  uint32_t h = ht_slot(id, size);
-  for (uint32_t probe = 0; probe < size; ++probe) {
-    uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
-    if (cur == kEmpty) return false;
-    if ((cur & ID_MASK) == id) return (atomicOr(&ht[h], EXPANDED) & EXPANDED) == 0;
-    if (++h == size) h = 0;
+    h = ht_next(h, st, size);
   }
   return false;
 }
@@ -264,8 +265,13 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   // visited set: shared memory sized for the expected visits; worst case in global memory
   uint64_t worst = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg;
   uint64_t expect = (uint64_t)cfg.init_num + (uint64_t)cfg.epochs * cfg.extend_to * maxdeg / 4;
-  uint64_t big = round_up(worst * 8 / 5 + 64, 256);
-  uint64_t small = std::min<uint64_t>(std::max<uint64_t>(round_up(expect * 8 / 5, 256), 2048), 12288);
+  auto nice = [](uint64_t x) {  // the next size of the form 2^k or 3 * 2^k (coprime with the probe steps)
+    uint64_t p = 256;
+    while (p < x && p * 3 / 2 < x) p *= 2;
+    return p >= x ? p : p * 3 / 2;
+  };
+  uint64_t big = nice(worst * 8 / 5 + 64);
+  uint64_t small = std::min<uint64_t>(std::max<uint64_t>(nice(expect * 8 / 5), 2048), 12288);
   small = std::min(small, big);
   if (big > (1ull << 28)) return fail(EFG_ERR_ARG, "search parameters visit too many candidates");
   // block size: 256 threads when several CTAs fit on an SM, else 512 threads

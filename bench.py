@@ -292,11 +292,110 @@ def run_gpu(args):
         line["bf16_learned"] = learned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
+    if not args.no_batching:
+        idx.close()
+        idx = None
+        line["batching"] = measure_batching(E, X, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    idx.close()
+    if idx is not None:
+        idx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+BATCH_GRAPH = dict(trees=8, merge_level=8, epochs=8, check=25, L=40, K=20, S=10)
+
+
+def measure_batching(E, X, args):
+    """The batching form's workload: the same 1M x 128 base with a K = 20 graph; held-out queries in
+    batches of lognormal size (median 256, clipped to [1, 8192]); per-query k uniform in
+    {1, 10, 50, 100}; per-query extend = scale * max(k, 10) and pool = U(6, 10) x extend, the scale
+    the smallest of a ladder reaching mean recall@k >= 0.95 on a 5000-query sample.  Every batch goes
+    through one captured search plan (CUDA graph; block size autotuned); host wall time per batch
+    (queries in, ids out) gives the latency percentiles."""
+    import torch
+    from efanna_gb300 import datasets
+    rng = np.random.default_rng(7)
+    n = args.n
+    t0 = time.perf_counter()
+    idx = E.Index.from_device(X.data_ptr(), n, 128, 128, E.IndexParams(**BATCH_GRAPH))
+    idx.build_index()
+    idx.build_trees(SEARCH_TREES)
+    idx.set_search_params(4, 1200, 200, SEARCH_TREES)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    total = args.batch_queries
+    q = datasets.mixture_u8(total, 128, seed=0, sample_seed=999)
+    sizes, s_ = [], 0
+    while s_ < total:
+        b = int(np.clip(np.round(rng.lognormal(np.log(256.0), 1.0)), 1, 8192))
+        b = min(b, total - s_)
+        sizes.append(b)
+        s_ += b
+    ks = rng.choice(np.array([1, 10, 50, 100]), total)
+    ratio = rng.uniform(6.0, 10.0, total)
+    sub = np.sort(rng.choice(total, min(5000, total), replace=False))
+    Qs = torch.from_numpy(q[sub]).cuda()
+    gts = torch.zeros((len(sub), 100), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), n, 128, 128, Qs.data_ptr(), len(sub), 128, 100, gts.data_ptr())
+    torch.cuda.synchronize()
+    gts = gts.cpu().numpy()
+
+    def params(scale_of_k):
+        sc = np.array([scale_of_k[int(k)] for k in ks])
+        ext = np.maximum(np.ceil(sc * np.maximum(ks, 10)), ks).astype(np.int64)
+        pool = np.minimum(np.ceil(ratio * ext), n).astype(np.int64)
+        return np.stack([np.full(total, 8), pool, ext, ks], 1).astype(np.int32)
+
+    # autotune the extend scale per k: the smallest of the ladder with recall@k >= 0.95 in that group
+    scales = (1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 16.0, 24.0, 32.0, 48.0, 64.0)
+    chosen, ladder = {}, []
+    for kv in (1, 10, 50, 100):
+        grp = sub[ks[sub] == kv]
+        gpos = np.searchsorted(sub, grp)
+        for scale in scales:
+            p = params({1: scale, 10: scale, 50: scale, 100: scale})
+            try:
+                res = idx.knn_search_batch(q[grp], p[grp], 100)
+            except E.EfannaError as e:  # pool/extend beyond what one query's shared memory holds
+                ladder.append({"k": kv, "scale": scale, "error": str(e)[:80]})
+                break
+            rc = float(np.mean([len(set(r[:kv]) & set(g[:kv])) / kv for r, g in zip(res, gts[gpos])]))
+            ladder.append({"k": kv, "scale": scale, "recall@k": round(rc, 4)})
+            chosen[kv] = scale
+            if rc >= TARGET:
+                break
+    p = params(chosen)
+    res = idx.knn_search_batch(q[sub], p[sub], 100)
+    recall_all = float(np.mean([len(set(r[:k]) & set(g[:k])) / k for r, g, k in zip(res, gts, ks[sub])]))
+    limits = (int(p[:, 0].max()), int(p[:, 1].max()), int(p[:, 2].max()), 100)
+    plan = idx.search_plan(8192, limits, calib=q[:2048])
+    out = np.zeros((8192, 100), np.int32)
+    for w in range(3):
+        plan.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
+    lat, s_ = [], 0
+    t_all = time.perf_counter()
+    for b in sizes:
+        t0 = time.perf_counter()
+        plan.run(q[s_:s_ + b], p[s_:s_ + b], out[:b])
+        lat.append(time.perf_counter() - t0)
+        s_ += b
+    wall = time.perf_counter() - t_all
+    res = {"value": round(total / wall, 1), "unit": "queries/s", "queries": total, "batches": len(sizes),
+           "batch_latency_ms": {"p50": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                                "p99": round(float(np.percentile(lat, 99)) * 1e3, 3),
+                                "max": round(float(np.max(lat)) * 1e3, 3)},
+           "batch_size": {"median": int(np.median(sizes)), "max": int(max(sizes))},
+           "recall@k": round(recall_all, 4), "extend_scale_per_k": {str(k): v for k, v in chosen.items()},
+           "ladder": ladder,
+           "plan_threads": plan.threads, "graph": "K=20 (trees 8, ml 8, iter 8, L 40, check 25, S 10)",
+           "graph_build_s": round(build_s, 3),
+           "form": "per-query k in {1,10,50,100}, pool = U(6,10) x extend; one captured CUDA graph replayed "
+                   "per batch (host queries in, ids out), persistent kernel, autotuned block size"}
+    plan.close()
+    idx.close()
+    return res
 
 
 LEARNED_RUNGS = [(4, 600, 60), (6, 1200, 120), (6, 2000, 200), (8, 3000, 300), (8, 4000, 400),
@@ -450,6 +549,8 @@ def main():
     ap.add_argument("--point", type=int, nargs=3, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -241,6 +241,18 @@ def run_gpu(args):
     idx.set_search_precision("fp32")
     hbm, peak_kind = peaks()
 
+    traffic_file = os.path.join(ROOT, "profiles", "nnexp_traffic_1Mx128.json")
+    measured = json.load(open(traffic_file)) if os.path.exists(traffic_file) else None
+
+    def traffic_of(r):
+        """DRAM bytes per step from the committed ncu capture of this same workload, else None."""
+        if not measured:
+            return None
+        w = measured["workload"]
+        if (w["n"], w["queries"], tuple(w["point"])) != (args.n, nq, tuple(r["point"])):
+            return None
+        return measured["per_step_bytes"].get(r["precision"])
+
     def roofline(r):
         # one search launch per step (plus the overflow launch when queries overflow), timed on its stream
         achieved = r["bytes_q"] * nq / (r["per_step_ms"] / 1e3) / 1e9
@@ -248,7 +260,8 @@ def run_gpu(args):
                 "peak_kind": peak_kind + " (burst)", "unit": "GB/s", "frac": round(achieved / hbm, 4),
                 "algorithmic_bytes_per_query": round(r["bytes_q"], 1),
                 "distance_evals_per_query": round(r["evals_q"], 1), "expanded_per_query": round(r["exp_q"], 1),
-                "traffic": None}
+                "traffic": traffic_of(r), "traffic_unit": "bytes per step (main + overflow launch)",
+                "traffic_source": "profiles/nnexp_traffic_1Mx128.md (ncu dram__bytes_read/write on this workload)"}
 
     def point_of(r):
         pt = r["point"]

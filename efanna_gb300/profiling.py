@@ -2,7 +2,8 @@
 
     python -m efanna_gb300.profiling table <ncu.csv>        per-kernel launch counts, time, share
     python -m efanna_gb300.profiling search [--n N] [--nq Q] [--point E P X] [--trees T]
-                                            [--precision fp32|bf16 ...] [--repeat R]
+                                            [--precision fp32|bf16|fp8 ...] [--repeat R]
+                                            [--method 0|1] [--recall]
         builds a graph on the seeded mixture and runs batched searches (R per precision and
         point): the small case used for Nsight Compute captures of nnexp_kernel (N=400k keeps
         the base above the L2 size).
@@ -13,6 +14,8 @@ import argparse
 import collections
 import csv
 import sys
+
+import numpy as np
 
 _SCALE = {"ns": 1e-6, "nsecond": 1e-6, "us": 1e-3, "usecond": 1e-3, "ms": 1.0, "msecond": 1.0, "s": 1e3,
           "second": 1e3}
@@ -40,7 +43,21 @@ def launch_table(path: str, metric: str = "gpu__time_duration.sum"):
     return "\n".join(out)
 
 
-def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2) -> None:
+def idx_exact(x, q):
+    """Exact 10-NN on the GPU (the library's brute force)."""
+    import torch
+
+    import efanna_gb300 as E
+    X, Q = torch.from_numpy(x).cuda(), torch.from_numpy(q).cuda()
+    out = torch.zeros((q.shape[0], 10), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), x.shape[0], x.shape[1], x.shape[1], Q.data_ptr(), q.shape[0], q.shape[1],
+                             10, out.data_ptr())
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2,
+                method: int = 0, recall: bool = False) -> None:
     import time
 
     import efanna_gb300 as E
@@ -51,18 +68,24 @@ def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp3
     idx.build_index()
     idx.build_trees(trees)
     pts = [point] + list(extra or [])
+    gt = None
+    if recall:
+        gt = idx_exact(x, q)
     for prec in precisions:
         idx.set_search_precision(prec)
         for pt in pts:
-            idx.set_search_params(pt[0], pt[1], pt[2], trees)
             for _ in range(repeat):
+                idx.set_search_params(pt[0], pt[1], pt[2], trees, -1, method)  # kgraph enlarges the pool
                 t0 = time.perf_counter()
-                idx.knn_search(10, q)
+                res = idx.knn_search(10, q)
                 s = idx.search_stats()
-                print("search %s %d/%d/%d, %d queries: %.3f ms kernel (%d launches), %.1f evals/query, "
-                      "%.1f expanded/query, %d overflow, wall %.3f s" %
-                      (prec, pt[0], pt[1], pt[2], nq, s.device_ms, s.kernel_launches, s.distance_evals / nq,
-                       s.expanded_nodes / nq, s.overflow_queries, time.perf_counter() - t0))
+                wall = time.perf_counter() - t0
+                rec = "" if gt is None else ", recall@10 %.4f" % np.mean(
+                    [len(set(r) & set(g)) / 10 for r, g in zip(res, gt)])
+                print("search %s method %d %d/%d/%d, %d queries: %.3f ms kernel (%d launches), %.1f evals/query, "
+                      "%.1f expanded/query, %d overflow, wall %.3f s%s" %
+                      (prec, method, pt[0], pt[1], pt[2], nq, s.device_ms, s.kernel_launches, s.distance_evals / nq,
+                       s.expanded_nodes / nq, s.overflow_queries, wall, rec))
 
 
 if __name__ == "__main__":
@@ -79,11 +102,13 @@ if __name__ == "__main__":
                    help="further epochs/pool/extend points to time after --point")
     s.add_argument("--precision", nargs="+", default=["fp32"], choices=["fp32", "bf16", "fp8"])
     s.add_argument("--repeat", type=int, default=2)
+    s.add_argument("--method", type=int, default=0, help="0 nnexp, 1 kgraph")
+    s.add_argument("--recall", action="store_true", help="also report recall@10 against the exact 10-NN")
     a = ap.parse_args()
     if a.cmd == "table":
         print(launch_table(a.csv))
     elif a.cmd == "search":
-        search_case(a.n, a.nq, a.point, a.trees, a.also, a.precision, a.repeat)
+        search_case(a.n, a.nq, a.point, a.trees, a.also, a.precision, a.repeat, a.method, a.recall)
     else:
         ap.print_help()
         sys.exit(1)

@@ -411,8 +411,10 @@ def measure_batching(E, X, args):
     return res
 
 
+# settings that all fit the two-CTA-per-SM layout of the plain operating point, so that a batch mixing
+# them runs with that layout (a larger top rung would size every query's shared memory for itself)
 LEARNED_RUNGS = [(4, 600, 60), (6, 1200, 120), (6, 2000, 200), (8, 3000, 300), (8, 4000, 400),
-                 (8, 6000, 600), (10, 9000, 900)]
+                 (8, 5000, 500), (8, 6000, 600)]
 
 
 def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args):

@@ -104,12 +104,6 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    return ws, rank
-
-
 def make_data(n, nq):
     from efanna_gb300 import datasets
     x = datasets.mixture_u8(n, 128, seed=0)
@@ -122,11 +116,9 @@ def run_gpu(args):
     import torch
     import efanna_gb300 as E
 
-    ws, rank = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+    from efanna_gb300 import replicas
+    ws, rank, _ = replicas.world()
+    replicas.init("nccl")
     dev = torch.device("cuda")
     x, q = make_data(args.n, args.nq)
     nq = q.shape[0]
@@ -207,22 +199,16 @@ def run_gpu(args):
         ev1 = torch.cuda.Event(enable_timing=True)
         clocks = ClockSampler()
         clocks.start()
-        if ws > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
             search_once(point)
         ev1.record(stream)
         torch.cuda.synchronize()
-        if ws > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         ck = clocks.stop()
-        ms = ev0.elapsed_time(ev1)
-        ms_t = torch.tensor([ms], device=dev)
-        if ws > 1:
-            torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(ms_t.item())
+        ms = replicas.max_over_ranks(ev0.elapsed_time(ev1), dev)
         # end to end through the host API (queries host->device, ids device->host inside the region)
         for _ in range(max(1, args.warmup // 2)):
             idx.knn_search(10, q)
@@ -232,7 +218,8 @@ def run_gpu(args):
         e2e_s = time.perf_counter() - t0
         return {"precision": precision, "point": point, "ladder": ladder, "config_recall": res_cfg,
                 "recall": recall(res_host, gt), "ms": ms, "per_step_ms": ms / args.steps,
-                "value": ws * nq * args.steps / (ms / 1e3), "e2e": ws * nq * args.steps / e2e_s,
+                "value": replicas.throughput(nq * args.steps, ms / 1e3, ws),
+                "e2e": replicas.throughput(nq * args.steps, replicas.max_over_ranks(e2e_s, dev), ws),
                 "evals_q": evals_q, "exp_q": exp_q, "bytes_q": bytes_q, "launches": int(st.kernel_launches),
                 "overflow": int(st.overflow_queries), "reranked": int(st.reranked), "clocks": ck}
 
@@ -313,8 +300,7 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if idx is not None:
         idx.close()
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish()
 
 
 BATCH_GRAPH = dict(trees=8, merge_level=8, epochs=8, check=25, L=40, K=20, S=10)
@@ -504,7 +490,8 @@ def cpu_baseline(x, q, gt, point, idx, args):
 
 # ------------------------------------------------------------------------------ reference arm
 def run_reference(args):
-    ws, rank = dist_env()
+    from efanna_gb300 import replicas
+    ws, rank, _ = replicas.world()
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))

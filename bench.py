@@ -483,9 +483,33 @@ def cpu_baseline(x, q, gt, point, idx, args):
     res = O.search(x, forest, gp, gi, q[:ns], k=10, epochs=point[0], init_num=point[1], extend_to=point[2],
                    trees=SEARCH_TREES, mode=O.OMP, threads=cores)
     dt = time.perf_counter() - t0
+    n1 = max(1, ns // 10)  # the same search on one core ("without parallelism"), a tenth of the sample
+    t0 = time.perf_counter()
+    O.search(x, forest, gp, gi, q[:n1], k=10, epochs=point[0], init_num=point[1], extend_to=point[2],
+             trees=SEARCH_TREES, mode=O.OMP, threads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": round(ns / dt, 1), "unit": "queries/s", "cores": cores, "kind": "port",
             "sample": "%d of %d queries, same trees/graph/operating point, OpenMP nnexp restatement" % (ns, len(q)),
-            "recall@10": round(recall(res, gt[:ns]), 4)}
+            "recall@10": round(recall(res, gt[:ns]), 4), "cpu_model": cpu_model(),
+            "omp_threads": cores, "single_thread": {"value": round(n1 / dt1, 1), "sample": "%d queries" % n1}}
+
+
+def cpu_model() -> str:
+    """The host CPU's model string (from /proc/cpuinfo), else the platform's processor name."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+        import subprocess as sp
+        out = sp.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 # ------------------------------------------------------------------------------ reference arm
@@ -534,7 +558,8 @@ def run_reference(args):
             "build": {"graph_build_s": round(build_s, 3), "search_trees16_s": round(trees_s, 3), "status": rc},
             "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": cores, "kind": "port",
                              "sample": "%d queries per step; index built by the OpenMP restatement of the "
-                                       "reference on the same host" % ns},
+                                       "reference on the same host" % ns, "cpu_model": cpu_model(),
+                             "omp_threads": int(os.environ.get("OMP_NUM_THREADS", cores))},
             "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -446,7 +446,6 @@ struct efg_learned {
   DevBuf<double> loss;
   DevBuf<uint32_t> pred_c, pred_r, seeds, batch_rows;
   DevBuf<efg_query_params> qp, ladder;
-  DevBuf<int32_t> out_scratch;
   efg_learned_stats stats{};
 };
 
@@ -668,7 +667,7 @@ void efg_learned_destroy(efg_learned* L) {
   L->wb.release(); L->tclusters.release(); L->tlabel.release(); L->trainq.release(); L->xb.release();
   L->h1b.release(); L->h2b.release(); L->h1.release(); L->h2.release(); L->z.release(); L->dz.release();
   L->dh2.release(); L->dh1.release(); L->loss.release(); L->pred_c.release(); L->pred_r.release();
-  L->seeds.release(); L->batch_rows.release(); L->qp.release(); L->ladder.release(); L->out_scratch.release();
+  L->seeds.release(); L->batch_rows.release(); L->qp.release(); L->ladder.release();
   delete L;
 }
 

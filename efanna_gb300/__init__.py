@@ -148,7 +148,7 @@ def lib():
         "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_knn_search_batch": (i32, [vp, f32p, u64, u32, u64, vp, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
-        "efg_knn_search_seeded_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, u32, vp, vp]),
+        "efg_knn_search_seeded_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, u32, i32, vp, vp]),
         "efg_search_plan_create": (i32, [vp, u64, C.POINTER(QueryParams), f32p, u64, C.POINTER(vp)]),
         "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_threads": (i32, [vp]),
@@ -166,6 +166,12 @@ def lib():
         "efg_learned_grad": (i32, [vp, vp, u32, u64, vp, vp, C.POINTER(C.c_double), f32p]),
         "efg_learned_clusters": (i32, [vp, vp, vp, vp]),
         "efg_learned_destroy": (None, [vp]),
+        "efg_hash_create": (i32, [vp, vp, u32, u32, u32, C.POINTER(vp)]),
+        "efg_hash_ball_size": (u64, [vp]),
+        "efg_hash_seeds_device": (i32, [vp, vp, u64, u64, u32, vp, vp]),
+        "efg_hash_search_device": (i32, [vp, vp, vp, u64, u64, vp, u64, u32, vp, vp]),
+        "efg_hash_search": (i32, [vp, vp, f32p, u64, u32, u64, vp, u32, vp]),
+        "efg_hash_destroy": (None, [vp]),
         "efg_nnd_init": (i32, [vp, C.POINTER(HostState)]),
         "efg_nnd_iterate": (i32, [vp, C.POINTER(HostState), u32, C.POINTER(C.c_uint64)]),
     }
@@ -283,12 +289,12 @@ class Index:
                                                  C.c_void_p(stream)))
 
     def knn_search_seeded_device(self, q_ptr: int, nq: int, row_stride: int, params_ptr: int, limits, seeds_ptr: int,
-                                 seeds_per_query: int, out_ptr: int, stream: int = 0):
+                                 seeds_per_query: int, out_ptr: int, stream: int = 0, use_trees: bool = True):
         lim = QueryParams(*[int(v) for v in limits])
         _check(lib().efg_knn_search_seeded_device(self._h, C.c_void_p(q_ptr), nq, row_stride,
                                                   C.c_void_p(params_ptr or None), C.byref(lim),
-                                                  C.c_void_p(seeds_ptr), seeds_per_query, C.c_void_p(out_ptr),
-                                                  C.c_void_p(stream)))
+                                                  C.c_void_p(seeds_ptr), seeds_per_query, int(use_trees),
+                                                  C.c_void_p(out_ptr), C.c_void_p(stream)))
 
     def search_plan(self, capacity: int, limits, calib: np.ndarray | None = None) -> "SearchPlan":
         return SearchPlan(self, capacity, limits, calib)
@@ -468,6 +474,59 @@ class Learned:
     def close(self):
         if self._h:
             lib().efg_learned_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HashTables:
+    """The hashing initialiser's tables (efg_hash) over an Index's base, for the hashing-seeded
+    search (HASHINGIndex with search method 1, algorithm/hashing_index.hpp:1087-1200).  ``codes`` is
+    tables x n codes of ``code_bits`` bits; the search uses the index's graph and its search
+    parameters (epochs, pool, extend), and no trees."""
+
+    def __init__(self, index: "Index", codes: np.ndarray, code_bits: int, radius: int):
+        c = np.ascontiguousarray(codes, dtype=np.uint64)
+        if c.ndim != 2 or c.shape[1] != index.n:
+            raise ValueError("codes must be tables x n")
+        self.index, self.tables, self.code_bits, self.radius = index, c.shape[0], code_bits, radius
+        h = C.c_void_p()
+        _check(lib().efg_hash_create(index._h, C.c_void_p(c.ctypes.data), c.shape[0], code_bits, radius,
+                                     C.byref(h)))
+        self._h = h
+
+    @property
+    def ball_size(self) -> int:
+        return int(lib().efg_hash_ball_size(self._h))
+
+    def search(self, k: int, queries: np.ndarray, qcodes: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        qc = np.ascontiguousarray(qcodes, dtype=np.uint64)
+        if qc.shape != (self.tables, q.shape[0]):
+            raise ValueError("qcodes must be tables x nq")
+        out = np.zeros((q.shape[0], k), dtype=np.int32)
+        _check(lib().efg_hash_search(self.index._h, self._h, _fp(q), q.shape[0], q.shape[1], q.shape[1],
+                                     C.c_void_p(qc.ctypes.data), k, C.c_void_p(out.ctypes.data)))
+        return out
+
+    def search_device(self, q_ptr: int, nq: int, row_stride: int, qcodes_ptr: int, qcode_stride: int, k: int,
+                      out_ptr: int, stream: int = 0):
+        _check(lib().efg_hash_search_device(self.index._h, self._h, C.c_void_p(q_ptr), nq, row_stride,
+                                            C.c_void_p(qcodes_ptr), qcode_stride, k, C.c_void_p(out_ptr),
+                                            C.c_void_p(stream)))
+
+    def seeds_device(self, qcodes_ptr: int, qcode_stride: int, nq: int, seeds_per_query: int, out_ptr: int,
+                     stream: int = 0):
+        _check(lib().efg_hash_seeds_device(self._h, C.c_void_p(qcodes_ptr), qcode_stride, nq, seeds_per_query,
+                                           C.c_void_p(out_ptr), C.c_void_p(stream)))
+
+    def close(self):
+        if self._h:
+            lib().efg_hash_destroy(self._h)
             self._h = None
 
     def __del__(self):

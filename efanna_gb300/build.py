@@ -18,7 +18,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libefanna_gb300.so")
 CLI_SRC = os.path.join(HERE, "cli", "efg_cli.cc")
 CLI = os.path.join(HERE, "cli", "efg_cli")
-SOURCES = ["index.cu", "distance.cu", "search.cu", "kgraph.cu", "plan.cu", "learned.cu", "trees.cu", "nndescent.cu", "noalloc.cu"]
+SOURCES = ["index.cu", "distance.cu", "search.cu", "kgraph.cu", "plan.cu", "learned.cu", "hashing.cu", "trees.cu", "nndescent.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -393,12 +393,13 @@ int efg_knn_search_batch_device(efg_index* idx, const float* d_q, uint64_t nq, u
 
 int efg_knn_search_seeded_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t row_stride,
                                  const efg_query_params* d_params, const efg_query_params* limits,
-                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int32_t* d_out, void* stream) {
+                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int use_trees, int32_t* d_out,
+                                 void* stream) {
   if (!idx || !limits || ((!d_q || !d_out || (!d_seeds && seeds_per_query)) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   if (idx->sp.method != 0) return fail(EFG_ERR_ARG, "seeded search uses search method 0");
   return search_device_ex(idx, d_q, nq, row_stride, *limits, d_params, nullptr, d_out, (cudaStream_t)stream, false,
-                          d_seeds, seeds_per_query);
+                          d_seeds, seeds_per_query, use_trees != 0);
 }
 
 int efg_knn_search_batch(efg_index* idx, const float* q, uint64_t nq, uint32_t dim, uint64_t row_stride,

@@ -382,18 +382,23 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
 
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
-                     bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query) {
+                     bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query, bool use_trees) {
   const SearchParams& sp = idx->sp;
   const uint32_t k = lim.k;
-  EFG_TRY(search_common_checks(idx, k));
+  if (use_trees) {
+    EFG_TRY(search_common_checks(idx, k));
+  } else {  // a pool from the seeds alone (then the random fill): no trees needed
+    if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
+    if (k == 0) return fail(EFG_ERR_ARG, "k must be positive");
+  }
   if (lim.init_num <= 0 || (uint64_t)lim.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
   if (lim.epochs < 0 || lim.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
   if ((int)k > lim.init_num) return fail(EFG_ERR_ARG, "k must be in [1, pool size]");
   if (nq == 0) return EFG_OK;
 
   SearchCfg cfg{};
-  cfg.T = (uint32_t)sp.search_trees;
-  cfg.lsize = (uint32_t)lim.init_num * 2 / (5 * cfg.T) + 1;
+  cfg.T = use_trees ? (uint32_t)sp.search_trees : 0;
+  cfg.lsize = cfg.T ? (uint32_t)lim.init_num * 2 / (5 * cfg.T) + 1 : 0;
   cfg.init_num = (uint32_t)lim.init_num;
   cfg.extend_to = std::min<uint32_t>((uint32_t)lim.extend_to, cfg.init_num);
   cfg.result_size = std::max<uint32_t>(cfg.extend_to, k);

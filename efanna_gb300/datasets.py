@@ -63,3 +63,23 @@ def mixture_unit(n: int, d: int = 960, n_comp: int = 32, block: int = 16, seed: 
         g /= g.sum(axis=2, keepdims=True)
         out[s:e] = g.reshape(e - s, d)
     return out
+
+
+def sign_codes(x: np.ndarray, tables: int, bits: int, seed: int = 0, center: np.ndarray | None = None,
+               chunk: int = 1 << 16) -> np.ndarray:
+    """Binary codes for the hashing-seeded search: per table, ``bits`` seeded random hyperplanes
+    through ``center`` (pass the base's mean for base and queries alike); bit b of a code is set
+    where the point lies on the positive side of hyperplane b.  Returns tables x n uint64."""
+    x = np.asarray(x, dtype=np.float32)
+    if center is None:
+        center = x.mean(0)
+    rng = np.random.default_rng(seed)
+    planes = rng.standard_normal((tables, x.shape[1], bits)).astype(np.float32)
+    weights = (np.uint64(1) << np.arange(bits, dtype=np.uint64))
+    out = np.empty((tables, x.shape[0]), dtype=np.uint64)
+    for s in range(0, x.shape[0], chunk):
+        xc = x[s:s + chunk] - center
+        for t in range(tables):
+            side = (xc @ planes[t]) > 0
+            out[t, s:s + chunk] = (side.astype(np.uint64) * weights).sum(1, dtype=np.uint64)
+    return out

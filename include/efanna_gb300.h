@@ -153,14 +153,17 @@ int efg_knn_search_batch_device(efg_index* idx, const float* d_queries, uint64_t
                                 const efg_query_params* d_params, const efg_query_params* limits,
                                 int32_t* d_out_ids, const uint32_t* d_nq, void* stream);
 
-/* Seeded batch (the learned form's search): like efg_knn_search_batch_device, and each query's pool
- * starts with its seeds_per_query entry ids from d_seeds (row qi, in order; ids >= n and repeats are
- * skipped), followed by the tree leaves as usual until the query's pool size.  d_params may be NULL
- * (every query at *limits). */
+/* Seeded batch: like efg_knn_search_batch_device, and each query's pool starts with its
+ * seeds_per_query entry ids from d_seeds (row qi, in order; ids >= n and repeats are skipped).
+ * use_trees != 0: the tree leaves follow as usual until the query's pool size (the learned form's
+ * search).  use_trees == 0: no trees are needed or read; a pool the seeds leave short is topped up
+ * by the random fill -- the search of the hashing initialiser (getNeighborsIEH32_nnexp,
+ * algorithm/hashing_index.hpp:1087-1200), whose Hamming-ball bucket visits give the seed order.
+ * d_params may be NULL (every query at *limits). */
 int efg_knn_search_seeded_device(efg_index* idx, const float* d_queries, uint64_t nq, uint64_t row_stride,
                                  const efg_query_params* d_params, const efg_query_params* limits,
-                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int32_t* d_out_ids,
-                                 void* stream);
+                                 const uint32_t* d_seeds, uint32_t seeds_per_query, int use_trees,
+                                 int32_t* d_out_ids, void* stream);
 
 /* Learned form (no reference counterpart).  A two-layer MLP (d -> hidden -> hidden -> clusters +
  * rungs; BF16 weights and activations, FP32 accumulation; trained on the device by the library's own
@@ -221,6 +224,37 @@ int efg_learned_grad(efg_learned* lr, const float* d_x, uint32_t B, uint64_t row
  * entries_per_cluster, 0xffffffff past the count) and counts; any pointer may be NULL. */
 int efg_learned_clusters(efg_learned* lr, int32_t* host_assign, uint32_t* host_entries, uint32_t* host_counts);
 void efg_learned_destroy(efg_learned* lr);
+
+/* Hashing-seeded search: the reference's hashing initialiser (HASHINGIndex, search method 1 there:
+ * getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp, algorithm/hashing_index.hpp:1087-1200 and
+ * 1354-1470).  Every base point has one binary code per hash table (made outside the library, as in
+ * the reference; io.read_codes reads its code files).  A query's pool is the first init_num distinct
+ * ids met while visiting its Hamming ball of the given radius -- radius by radius, each radius's
+ * flipped-bit tuples in ascending lexicographic order, all tables at every mask, bucket members in
+ * ascending id order -- topped up by the random fill, then expanded over the graph with the index's
+ * search parameters (epochs, init_num, extend_to; no trees are needed).
+ * efg_hash_create: codes = tables x n codes (host, table-major) of code_bits bits (<= 64; the
+ * reference's code length after its shift), radius <= min(13, code_bits), Hamming ball x tables <=
+ * 2^26 probes.  The tables belong to idx, which must outlive them. */
+typedef struct efg_hash efg_hash;
+int efg_hash_create(efg_index* idx, const uint64_t* codes, uint32_t tables, uint32_t code_bits, uint32_t radius,
+                    efg_hash** out);
+/* Masks in the Hamming ball: sum over r <= radius of C(code_bits, r) (the reference's MaxCheck). */
+uint64_t efg_hash_ball_size(const efg_hash* h);
+/* Probe sequence of nq queries: d_qcodes[t * qcode_stride + q] is query q's code in table t;
+ * row q of d_seeds (seeds_per_query entries) receives the probe sequence's first entries,
+ * 0xffffffff past its end.  seeds_per_query = init_num * tables always holds the first init_num
+ * distinct ids. */
+int efg_hash_seeds_device(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_stride, uint64_t nq,
+                          uint32_t seeds_per_query, uint32_t* d_seeds, void* stream);
+/* The hashing-seeded search over device queries and codes: nq rows of k ids into d_out. */
+int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_queries, uint64_t nq, uint64_t row_stride,
+                           const uint64_t* d_qcodes, uint64_t qcode_stride, uint32_t k, int32_t* d_out_ids,
+                           void* stream);
+/* Host-memory form (qcodes: tables x nq); the results are kept for efg_save_results. */
+int efg_hash_search(efg_index* idx, efg_hash* h, const float* queries, uint64_t nq, uint32_t dim,
+                    uint64_t row_stride, const uint64_t* qcodes, uint32_t k, int32_t* out_ids);
+void efg_hash_destroy(efg_hash* h);
 
 /* A search plan: the batched nnexp launch sequence for up to `capacity` queries whose parameters
  * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers.  When

@@ -9,6 +9,10 @@
 //   IndexParams / SearchParams / init_algorithm / ValueType / ExtraParamsMap
 //                         general/params.hpp:7-42
 //   KDTreeUbIndexParams   algorithm/kdtreeub_index.hpp:14-35
+//   HASHINGIndexParams    algorithm/hashing_index.hpp:19-46 (the hashing initialiser: its code
+//                         files, hash tables and the pool/extend search seeded from them, search
+//                         method 1 there; its kgraph search, method 0, and its graph-less bucket
+//                         search are not provided and throw)
 //   Matrix                general/matrix.hpp:12-72
 //   Distance, L2Distance, L2DistanceSSE, L2DistanceAVX, L2DistanceAVXr4
 //                         general/distance.hpp:46-379 (here plain C++; the GPU computes the
@@ -23,6 +27,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <iostream>
 #include <map>
 #include <stdexcept>
@@ -153,6 +158,28 @@ struct KDTreeUbIndexParams : public IndexParams {
   }
 };
 
+struct HASHINGIndexParams : public IndexParams {
+  HASHINGIndexParams(int codelen, int TableNum, int UpperBits, int HashRadius, char*& BaseCodeFile,
+                     char*& QueryCodeFile, int codelenShift = 0) {
+    init_index_type = HASHING;
+    ValueType v;
+    v.int_val = codelen;
+    extra_params.insert(std::make_pair("codelen", v));
+    v.int_val = TableNum;
+    extra_params.insert(std::make_pair("tablenum", v));
+    v.int_val = UpperBits;
+    extra_params.insert(std::make_pair("upbits", v));
+    v.int_val = HashRadius;
+    extra_params.insert(std::make_pair("radius", v));
+    v.str_pt = BaseCodeFile;
+    extra_params.insert(std::make_pair("bcfile", v));
+    v.str_pt = QueryCodeFile;
+    extra_params.insert(std::make_pair("qcfile", v));
+    v.int_val = codelenShift;
+    extra_params.insert(std::make_pair("lenshift", v));
+  }
+};
+
 // ---- Matrix (general/matrix.hpp): a non-owning row view with the reference's padding rule -------
 template <typename T>
 class Matrix {
@@ -196,10 +223,13 @@ class FIndex {
   FIndex(const Matrix<DataType>& features, Distance<DataType>* d, const IndexParams& params)
       : index_params_(params), distance_(d), idx_(nullptr) {
     static_assert(sizeof(DataType) == 4, "efanna_gb300 indexes float vectors");
-    if (params.init_index_type != KDTREE_UB)
-      throw std::runtime_error("efanna_gb300 provides the KD-tree (KDTREE_UB) initialisation only");
     efg_build_params p;
     efg_default_build_params(&p);
+    if (params.init_index_type == HASHING) {
+      init_hashing(features, params, p);
+      return;
+    }
+    if (params.init_index_type != KDTREE_UB) throw std::runtime_error("unknown initialisation type");
     p.K = (uint32_t)params.K;
     p.S = (uint32_t)params.S;
     p.L = (uint32_t)params.L;
@@ -215,9 +245,18 @@ class FIndex {
     check(efg_index_create(reinterpret_cast<const float*>(features.data()), features.get_rows(),
                            (uint32_t)features.get_cols(), features.get_stride(), &p, &idx_));
   }
-  virtual ~FIndex() { efg_index_destroy(idx_); }
+  virtual ~FIndex() {
+    efg_hash_destroy(hash_);
+    efg_index_destroy(idx_);
+  }
 
   void buildIndex() {
+    if (hashing_) {  // HASHINGIndex::buildIndexImpl: the hash tables (hashing_index.hpp:872-886)
+      efg_hash_destroy(hash_);
+      hash_ = nullptr;
+      check(efg_hash_create(idx_, base_codes_.data(), (uint32_t)tables_, (uint32_t)bits_, (uint32_t)radius_, &hash_));
+      return;
+    }
     int rc = efg_build_graph(idx_);
     if (rc == EFG_ERR_MERGE_LEVEL) {
       efg_build_stats s;
@@ -227,8 +266,14 @@ class FIndex {
     }
     check(rc);
   }
-  void buildTrees() { check(efg_build_trees(idx_)); }
+  void buildTrees() {
+    if (!hashing_) check(efg_build_trees(idx_));  // the hashing initialiser has no trees
+  }
   void knnSearch(int k, const Matrix<DataType>& query) {
+    if (hashing_) {
+      hashing_search(k, query);
+      return;
+    }
     std::vector<int32_t> out((size_t)query.get_rows() * (size_t)k);
     int rc = efg_knn_search(idx_, reinterpret_cast<const float*>(query.data()), query.get_rows(),
                             (uint32_t)query.get_cols(), query.get_stride(), (uint32_t)k, out.data());
@@ -250,6 +295,7 @@ class FIndex {
   void saveResults(char* filename) { file(efg_save_results(idx_, filename), -10086); }
   void setSearchParams(int epochs, int init_num, int extend_to, int search_trees = 0, int search_lv = -1,
                        int search_method = 0) {
+    method_ = search_method;
     check(efg_set_search_params(idx_, epochs, init_num, extend_to, search_trees, search_lv, search_method));
   }
   size_t getGraphSize() { return (size_t)efg_graph_size(idx_); }
@@ -279,9 +325,92 @@ class FIndex {
     }
     check(rc);
   }
+  // HASHINGIndex's constructor (hashing_index.hpp:66-198): parameters, the radius limit per code
+  // length, and the base and query code files read at construction.
+  void init_hashing(const Matrix<DataType>& features, const IndexParams& params, efg_build_params& p) {
+    hashing_ = true;
+    auto get = [&](const char* key) -> const ValueType* {
+      ExtraParamsMap::const_iterator it = params.extra_params.find(key);
+      return it == params.extra_params.end() ? nullptr : &it->second;
+    };
+    const ValueType *len = get("codelen"), *tab = get("tablenum"), *up = get("upbits"), *rad = get("radius"),
+                    *bcf = get("bcfile"), *qcf = get("qcfile"), *sh = get("lenshift");
+    if (!len || !tab || !up || !rad || !bcf || !qcf)
+      throw std::runtime_error("HASHINGIndexParams: code length, tables, upper bits, radius and code files are required");
+    int codelen = len->int_val, shift = sh ? sh->int_val : 0;
+    tables_ = tab->int_val;
+    if (codelen > 64 || codelen < 1) throw std::runtime_error("code length not supported yet!");
+    if (tables_ < 1) throw std::runtime_error("Total hash table num error!");
+    if (codelen - shift <= 0) throw std::runtime_error("lenShift error: could not be larger than the code length!");
+    if (up->int_val >= codelen - shift) throw std::runtime_error("upbits should be smaller than the actual codelength!");
+    int actual = codelen - shift;
+    int cap = actual <= 32 ? 13 : actual <= 36 ? 11 : actual <= 40 ? 10 : actual <= 48 ? 9 : actual <= 60 ? 8 : 7;
+    radius_ = std::min(rad->int_val, cap);
+    int file_len = 0;
+    base_codes_ = load_codes(bcf->str_pt, codelen, shift, features.get_rows(), file_len);
+    query_codes_ = load_codes(qcf->str_pt, codelen, shift, 0, file_len);
+    bits_ = file_len - shift;  // the files' code length, as the reference's loader takes it
+    if (bits_ < 1 || bits_ > 64) throw std::runtime_error("code length not supported yet!");
+    if (radius_ > bits_) radius_ = bits_;
+    check(efg_index_create(reinterpret_cast<const float*>(features.data()), features.get_rows(),
+                           (uint32_t)features.get_cols(), features.get_stride(), &p, &idx_));
+  }
+  // LoadCode32 / LoadCode64 (hashing_index.hpp:206-300): files <prefix>_1 .. <prefix>_<tables>, each
+  // int32 1, int32 code length, int32 count, then count codes of 32 (code length <= 32) or 64 bits,
+  // shifted right by the shift and bounded by codelen - shift bits.  Returns tables x count codes.
+  std::vector<uint64_t> load_codes(const char* prefix, int codelen, int shift, size_t expect, int& file_len) {
+    std::vector<uint64_t> all;
+    size_t count = 0;
+    const uint64_t maxv = codelen - shift >= 64 ? ~0ull : (1ull << (codelen - shift)) - 1;
+    for (int t = 0; t < tables_; ++t) {
+      std::string path = std::string(prefix) + "_" + std::to_string(t + 1);
+      std::ifstream in(path.c_str(), std::ios::binary);
+      if (!in.is_open()) throw std::runtime_error("open file " + path + " error");
+      int head[3] = {0, 0, 0};
+      in.read(reinterpret_cast<char*>(head), sizeof(head));
+      if (!in || head[0] != 1 || head[2] < 0) throw std::runtime_error("codefile " + path + " error!");
+      file_len = head[1];
+      if (t == 0) count = (size_t)head[2];
+      if ((size_t)head[2] != count || (expect && count != expect))
+        throw std::runtime_error("codefile " + path + ": wrong number of codes");
+      for (size_t i = 0; i < count; ++i) {
+        uint64_t c = 0;
+        if (codelen <= 32) {
+          uint32_t w = 0;
+          in.read(reinterpret_cast<char*>(&w), 4);
+          c = w;
+        } else {
+          in.read(reinterpret_cast<char*>(&c), 8);
+        }
+        if (!in) throw std::runtime_error("codefile " + path + " truncated");
+        c >>= shift;
+        if (c > maxv) throw std::runtime_error("codefile " + path + " error! Exceed maximum value");
+        all.push_back(c);
+      }
+    }
+    return all;
+  }
+  void hashing_search(int k, const Matrix<DataType>& query) {
+    if (efg_graph_size(idx_) == 0)
+      throw std::runtime_error("efanna_gb300 provides the hashing initialiser's search over a loaded graph only");
+    if (method_ != 1)
+      throw std::runtime_error("efanna_gb300 provides the hashing initialiser's search method 1 (pool/extend) only");
+    if (!hash_) throw std::runtime_error("buildIndex() builds the hash tables before searching");
+    const size_t nq = query.get_rows();
+    if (query_codes_.size() != nq * (size_t)tables_)
+      throw std::runtime_error("the query code files hold a different number of queries");
+    std::vector<int32_t> out(nq * (size_t)k);
+    check(efg_hash_search(idx_, hash_, reinterpret_cast<const float*>(query.data()), nq, (uint32_t)query.get_cols(),
+                          query.get_stride(), query_codes_.data(), (uint32_t)k, out.data()));
+  }
+
   IndexParams index_params_;
   Distance<DataType>* distance_;
-  efg_index* idx_;
+  efg_index* idx_ = nullptr;
+  efg_hash* hash_ = nullptr;
+  bool hashing_ = false;
+  int method_ = 0, tables_ = 0, bits_ = 0, radius_ = 0;
+  std::vector<uint64_t> base_codes_, query_codes_;
 };
 
 }  // namespace efanna

@@ -31,6 +31,7 @@
 #include <limits>
 #include <random>
 #include <set>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 #ifdef _OPENMP
@@ -1316,7 +1317,7 @@ static void search_one(const Data& X, const Forest& F, const uint64_t* gptr, con
   size_t N = X.n;
   std::vector<uint8_t> tbflag(N, 0), newflag(N, 1);
   unsigned T = (unsigned)a.trees;
-  unsigned lsize = a.init_num * 2 / (5 * T) + 1;
+  unsigned lsize = T ? a.init_num * 2 / (5 * T) + 1 : 0;  // T == 0: a pool from the seeds alone
   std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, tbflag, a.seeds,
                                     a.nseeds);
   unsigned resultSize = (unsigned)a.extend_to;
@@ -1666,7 +1667,12 @@ int orc_search_batch(const float* data, uint64_t n, uint32_t d, uint64_t ld, voi
                      uint64_t seed, int32_t* out) {
   Data X{data, n, d, ld, MODE_CANON};
   Forest* F = (Forest*)forest;
-  if (search_trees <= 0 || (size_t)search_trees > F->nodes.size()) return -1;
+  // search_trees == 0 (with seeds): no trees -- the hashing initialiser's search
+  if (search_trees < 0 || (search_trees == 0 && !seeds) || (F && (size_t)search_trees > F->nodes.size()) ||
+      (!F && search_trees > 0))
+    return -1;
+  Forest empty;
+  if (!F) F = &empty;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 16) num_threads(threads < 1 ? 1 : threads)
 #endif
@@ -1682,6 +1688,79 @@ int orc_search_batch(const float* data, uint64_t n, uint32_t d, uint64_t ld, voi
     std::vector<int32_t> row(k);
     search_one(X, *F, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, MODE_CANON, seed, row.data(), nullptr);
     for (uint32_t j = 0; j < k_max; ++j) out[(uint64_t)i * k_max + j] = j < k ? row[j] : -1;
+  }
+  return 0;
+}
+
+// ---- hashing-seeded search (algorithm/hashing_index.hpp) ----
+// Hamming-ball masks in the reference's order (generateMask32 / generateMask64, hashing_index.hpp:
+// 348-860): the zero mask, then for r = 1..radius every r-tuple of bit positions i < j < ... in
+// lexicographic order.
+static void hamming_masks(unsigned bits, unsigned radius, std::vector<uint64_t>& out) {
+  out.assign(1, 0);
+  std::vector<unsigned> pos;
+  for (unsigned r = 1; r <= radius && r <= bits; ++r) {
+    pos.resize(r);
+    for (unsigned t = 0; t < r; ++t) pos[t] = t;
+    for (;;) {
+      uint64_t m = 0;
+      for (unsigned t = 0; t < r; ++t) m |= 1ull << pos[t];
+      out.push_back(m);
+      int t = (int)r - 1;  // next tuple: bump the last position that can still move
+      while (t >= 0 && pos[t] == bits - r + (unsigned)t) --t;
+      if (t < 0) break;
+      ++pos[t];
+      for (unsigned u = (unsigned)t + 1; u < r; ++u) pos[u] = pos[u - 1] + 1;
+    }
+  }
+}
+
+// getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp (hashing_index.hpp:1087-1200, 1354-1470):
+// buckets keyed by the full code (the reference splits it into upper and lower bits for a two-level
+// lookup, which finds the same bucket), members in insertion (= id) order; per query, masks in
+// order and tables inner, first occurrences until init_num, then the random fill and the pool /
+// extend expansion of search_one with no trees.  bcodes: tables x n, qcodes: tables x nq.
+int orc_search_hashed(const float* data, uint64_t n, uint32_t d, uint64_t ld, const uint64_t* gptr,
+                      const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, const uint64_t* bcodes,
+                      const uint64_t* qcodes, uint32_t tables, uint32_t bits, uint32_t radius, int epochs,
+                      int init_num, int extend_to, uint32_t k, int mode, int threads, uint64_t seed, int32_t* out,
+                      uint64_t* evals) {
+  if (tables < 1 || bits < 1 || bits > 64 || init_num <= 0 || (uint64_t)init_num > n || k == 0 ||
+      k > (uint32_t)init_num || epochs < 0 || extend_to < 0)
+    return -1;
+  if (extend_to > init_num) extend_to = init_num;  // setSearchParams (base_index.hpp:156-157)
+  Data X{data, n, d, ld, mode};
+  std::vector<std::unordered_map<uint64_t, std::vector<uint32_t>>> tab(tables);
+  for (uint32_t h = 0; h < tables; ++h)
+    for (uint64_t i = 0; i < n; ++i) tab[h][bcodes[(uint64_t)h * n + i]].push_back((uint32_t)i);
+  std::vector<uint64_t> masks;
+  hamming_masks(bits, radius, masks);
+  Forest empty;
+  if (mode == MODE_SEQ) srand(1);
+#ifdef _OPENMP
+  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+#endif
+  for (long long i = 0; i < (long long)nq; ++i) {
+    std::vector<uint8_t> seen(n, 0);
+    std::vector<uint32_t> prefix;
+    for (size_t j = 0; j < masks.size() && prefix.size() < (size_t)init_num; ++j)
+      for (uint32_t h = 0; h < tables && prefix.size() < (size_t)init_num; ++h) {
+        auto it = tab[h].find(qcodes[(uint64_t)h * nq + i] ^ masks[j]);
+        if (it == tab[h].end()) continue;
+        for (size_t e = 0; e < it->second.size() && prefix.size() < (size_t)init_num; ++e) {
+          uint32_t id = it->second[e];
+          if (seen[id]) continue;
+          seen[id] = 1;
+          prefix.push_back(id);
+        }
+      }
+    SearchArgs a{epochs, init_num, extend_to, 0, k};
+    a.seeds = prefix.data();
+    a.nseeds = (unsigned)prefix.size();
+    uint64_t nd = 0;
+    search_one(X, empty, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, mode, seed, out + (uint64_t)i * k, &nd);
+    if (evals) evals[i] = nd;
   }
   return 0;
 }

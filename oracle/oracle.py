@@ -86,6 +86,9 @@ def lib():
         L.orc_search_kgraph.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, u64p, u32p, f32p,
                                         C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
                                         C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p, u64p]
+        L.orc_search_hashed.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, u64p, u32p, f32p, C.c_uint64,
+                                        C.c_uint64, u64p, u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int,
+                                        C.c_int, C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p, u64p]
         _lib = L
     return _lib
 
@@ -233,7 +236,8 @@ def search(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, init_num=1
 
 def search_batch(data, forest: Forest, gptr, gids, queries, params, k_max, trees=16, seeds=None, threads=1,
                  seed: int = 1998):
-    """Canonical nnexp with per-query (epochs, pool, extend, k) rows and optional entry seeds."""
+    """Canonical nnexp with per-query (epochs, pool, extend, k) rows and optional entry seeds;
+    trees=0 (forest may be None, seeds required) builds pools from the seeds and the random fill."""
     data = np.ascontiguousarray(data, np.float32)
     queries = np.ascontiguousarray(queries, np.float32)
     gptr = np.ascontiguousarray(gptr, np.uint64)
@@ -242,7 +246,8 @@ def search_batch(data, forest: Forest, gptr, gids, queries, params, k_max, trees
     nq = queries.shape[0]
     out = np.zeros((nq, k_max), np.int32)
     sp = None if seeds is None else np.ascontiguousarray(seeds, np.uint32).reshape(nq, -1)
-    rc = lib().orc_search_batch(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1], forest.h,
+    rc = lib().orc_search_batch(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1],
+                                None if forest is None else forest.h,
                                 _p(gptr, C.c_uint64), _p(gids, C.c_uint32), _p(queries, C.c_float), nq,
                                 queries.shape[1], _p(params, C.c_int32), k_max, trees,
                                 None if sp is None else _p(sp, C.c_uint32), 0 if sp is None else sp.shape[1],
@@ -271,3 +276,27 @@ def search_kgraph(data, forest: Forest, gptr, gids, queries, k=10, epochs=4, ini
     if rc != 0:
         raise ValueError("orc_search_kgraph rejected its arguments")
     return out, ev, pool.value
+
+
+def search_hashed(data, gptr, gids, queries, bcodes, qcodes, bits, radius, k=10, epochs=4, init_num=1200,
+                  extend_to=200, mode: int = CANON, threads: int = 1, seed: int = 1998):
+    """getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp (the hashing-seeded search).  bcodes:
+    tables x n, qcodes: tables x nq.  Returns (ids, evals per query)."""
+    data = np.ascontiguousarray(data, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    gptr = np.ascontiguousarray(gptr, np.uint64)
+    gids = np.ascontiguousarray(gids, np.uint32)
+    bcodes = np.ascontiguousarray(bcodes, np.uint64)
+    qcodes = np.ascontiguousarray(qcodes, np.uint64)
+    nq = queries.shape[0]
+    assert bcodes.shape == (qcodes.shape[0], data.shape[0]) and qcodes.shape[1] == nq
+    out = np.zeros((nq, k), np.int32)
+    ev = np.zeros(nq, np.uint64)
+    rc = lib().orc_search_hashed(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1],
+                                 _p(gptr, C.c_uint64), _p(gids, C.c_uint32), _p(queries, C.c_float), nq,
+                                 queries.shape[1], _p(bcodes, C.c_uint64), _p(qcodes, C.c_uint64), bcodes.shape[0],
+                                 bits, radius, epochs, init_num, extend_to, k, mode, threads, seed,
+                                 _p(out, C.c_int32), _p(ev, C.c_uint64))
+    if rc != 0:
+        raise ValueError("orc_search_hashed rejected its arguments")
+    return out, ev

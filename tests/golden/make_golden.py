@@ -15,7 +15,13 @@ across runs) on small seeded integer-valued data, and stores inputs and outputs:
                parameter set in KGRAPH_POINTS: the first call's ids and a second call's ids on the
                same index (the first call may enlarge the stored pool size).
 
-``--only-kgraph`` regenerates just the kgraph fixtures.
+  <case>_hashing.npz  the reference's hashing-seeded search (HASHINGIndex, search method 1, through
+               its FIndex API via oracle/ref_drivers/hashing_search.cc) on the case's graph file with
+               seeded sign-of-projection codes (datasets.sign_codes) written as the reference's code
+               files, for each parameter set in HASH_POINTS: the codes as read back (tables x n and
+               tables x nq, after the shift), the code length in effect and the ids.
+
+``--only-kgraph`` / ``--only-hashing`` regenerate just those fixtures.
 
 The data are stored (as uint8) rather than regenerated so that the fixtures do not depend on the
 platform's numpy.
@@ -50,6 +56,12 @@ CASES = {
 # pools the reference enlarges to epochs * extend.
 KGRAPH_POINTS = [(8, 4, 400, 50, 10), (8, 4, 100, 50, 10), (8, 3, 600, 40, 20), (4, 2, 150, 100, 10),
                  (8, 5, 200, 30, 5)]
+
+
+# hashing search points (code length, tables, upper bits, radius, shift, epochs, pool, extend, k):
+# 32- and 64-bit code files, a shift, pools filled from the buckets and pools the random fill tops up.
+HASH_POINTS = [(12, 2, 4, 2, 0, 4, 200, 40, 10), (40, 3, 8, 1, 0, 3, 150, 30, 10), (16, 2, 5, 3, 2, 2, 300, 300, 20),
+               (10, 1, 3, 2, 0, 4, 2500, 50, 10), (20, 4, 6, 1, 0, 4, 400, 60, 10)]
 
 
 def run(cmd, threads):
@@ -93,6 +105,27 @@ def make_kgraph(name, tmp):
                         **{"second_%d" % i: a for i, a in enumerate(second)})
 
 
+def make_hashing(name, tmp):
+    g = np.load(os.path.join(HERE, name + ".npz"))
+    x, q = g["base"].astype(np.float32), g["queries"].astype(np.float32)
+    base, qf, r = os.path.join(tmp, "b.fvecs"), os.path.join(tmp, "q.fvecs"), os.path.join(tmp, "r.ivecs")
+    io.write_fvecs(base, x)
+    io.write_fvecs(qf, q)
+    bpre, qpre = os.path.join(tmp, "bc"), os.path.join(tmp, "qc")
+    out = {"points": np.array(HASH_POINTS)}
+    for i, (clen, tables, up, rad, shift, ep, pool, ext, k) in enumerate(HASH_POINTS):
+        io.write_codes(bpre, datasets.sign_codes(x, tables, clen, seed=100 + i), clen)
+        io.write_codes(qpre, datasets.sign_codes(q, tables, clen, seed=100 + i, center=x.mean(0)), clen)
+        run([O.ref_bin("hashing_search", "strict"), base, os.path.join(HERE, name + ".graph"), qf, bpre, qpre, r,
+             str(clen), str(tables), str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k)], 1)
+        bc, bits = io.read_codes(bpre, tables, clen, shift)
+        qc, _ = io.read_codes(qpre, tables, clen, shift)
+        word = np.uint32 if bits <= 32 else np.uint64
+        out.update({"bcodes_%d" % i: bc.astype(word), "qcodes_%d" % i: qc.astype(word), "bits_%d" % i: bits,
+                    "results_%d" % i: io.read_ivecs(r)})
+    np.savez_compressed(os.path.join(HERE, name + "_hashing.npz"), **out)
+
+
 def exact_knn(x, k):
     xd = x.astype(np.float64)
     nrm = (xd * xd).sum(1)
@@ -131,11 +164,15 @@ if __name__ == "__main__":
     O.build()
     if not O.build_ref():
         sys.exit("reference sources not found; fixtures unchanged")
+    only = [a for a in sys.argv if a.startswith("--only-")]
     with tempfile.TemporaryDirectory() as tmp:
-        if "--only-kgraph" not in sys.argv:
+        if not only:
             for name, spec in CASES.items():
                 make_case(name, *spec, tmp)
-        for name in CASES:
-            make_kgraph(name, tmp)
-        if "--skip-100k" not in sys.argv and "--only-kgraph" not in sys.argv:
+        if not only or "--only-kgraph" in only:
+            for name in CASES:
+                make_kgraph(name, tmp)
+        if not only or "--only-hashing" in only:
+            make_hashing("small_d32", tmp)
+        if "--skip-100k" not in sys.argv and not only:
             ref_recall_100k(tmp)

@@ -32,3 +32,22 @@ def test_cli_builds_and_prints_usage(efg):
     assert r.returncode == 1 and "efanna_search" in r.stderr
     r = subprocess.run([cli, "evaluate"], capture_output=True, text=True)
     assert r.returncode == 255 and "gound_truth" in r.stdout
+
+
+def build_hashing_driver(efg, out_dir):
+    """oracle/ref_drivers/hashing_search.cc -- a program written against the reference's API
+    (HASHINGIndexParams, FIndex) -- compiled against the facade instead of the reference."""
+    src = os.path.join(ROOT, "oracle", "ref_drivers", "hashing_search.cc")
+    out = os.path.join(str(out_dir), "hashing_search_gb300")
+    cmd = ["g++", "-std=c++11", "-O1", "-w", "-I", os.path.join(ROOT, "include", "efanna_gb300"), src,
+           "-L", os.path.dirname(efg.LIB_PATH), "-lefanna_gb300", "-Wl,-rpath," + os.path.dirname(efg.LIB_PATH),
+           "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+def test_hashing_program_compiles_against_facade(efg, tmp_path):
+    out = build_hashing_driver(efg, tmp_path)
+    nm = subprocess.run(["nm", "-u", out], capture_output=True, text=True).stdout
+    assert "efg_hash_create" in nm and "efg_hash_search" in nm

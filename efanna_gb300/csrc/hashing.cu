@@ -261,6 +261,11 @@ int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64
   if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   if (qcode_stride < nq) return fail(EFG_ERR_ARG, "qcode_stride < nq");
   const SearchParams& sp = idx->sp;
+  if (sp.method == 0) {  // the hashing initialiser's kgraph search (its method 0)
+    KgSeedSource src{h, d_qcodes, qcode_stride, h->tables, &h->seeds};
+    return kgraph_search_device(idx, d_q, nq, row_stride, k, d_out, (cudaStream_t)stream, false, &src);
+  }
+  if (sp.method != 1) return fail(EFG_ERR_ARG, "no such searching method");
   if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
   if (nq == 0) return EFG_OK;
   efg_query_params lim{sp.epochs, sp.init_num, sp.extend_to, k};

@@ -148,9 +148,18 @@ int make_base8(efg_index* idx);
 // Screening distances of (query, id) pairs in a given precision (the search's gather).
 int screen_pairs(efg_index* idx, int precision, const float* d_q, uint64_t nq, uint64_t qld, const uint32_t* d_ids,
                  uint32_t m, float* d_out, cudaStream_t s);
-// kgraph.cu: search method 1 (getNeighbors_kgraph).
+// kgraph.cu: search method 1 (getNeighbors_kgraph).  With a seed source the pool comes from the
+// hash tables' probe sequence instead of the trees, and expansions visit whole graph rows (the
+// hashing initialiser's kgraph search, getNeighborsIEH32_kgraph).
+struct KgSeedSource {
+  efg_hash* h;
+  const uint64_t* d_qcodes;  // tables x qstride
+  uint64_t qstride;
+  uint32_t tables;
+  DevBuf<uint32_t>* buf;  // seed rows, grown as needed
+};
 int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
-                         cudaStream_t s, bool count_evals);
+                         cudaStream_t s, bool count_evals, const KgSeedSource* hs = nullptr);
 
 // nndescent.cu
 struct NNDState;

@@ -35,6 +35,7 @@ struct KgCfg {
   uint32_t ld4, words;       // float4 per base row; bitset words per warp (multiple of 4)
   uint32_t warp_bytes;       // shared memory per warp
   uint32_t o_list, o_res, o_res2;
+  uint32_t full_rows;        // 1: an expansion visits the whole graph row, else its first E ids
 };
 
 __device__ __forceinline__ uint64_t kmask(uint64_t x) { return x & ~KEXP; }
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
           row = gptr[node];
           deg = (uint32_t)(gptr[node + 1] - row);
         }
-        uint32_t maxM = min(c.E, deg);
+        uint32_t maxM = c.full_rows ? deg : min(c.E, deg);
         uint32_t nk = L;
         for (uint32_t m0 = 0; m0 < maxM; m0 += 32) {
           uint32_t mm = m0 + lane;
@@ -273,13 +274,18 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
 }  // namespace
 
 int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
-                         cudaStream_t s, bool count_evals) {
+                         cudaStream_t s, bool count_evals, const KgSeedSource* hs) {
   SearchParams& sp = idx->sp;
-  EFG_TRY(search_common_checks(idx, k));
+  if (hs) {  // pools from the hash tables: no trees needed
+    if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
+    if (k == 0) return fail(EFG_ERR_ARG, "k must be positive");
+  } else {
+    EFG_TRY(search_common_checks(idx, k));
+  }
   if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
   if (sp.epochs < 0 || sp.extend_to < 0) return fail(EFG_ERR_ARG, "negative epochs or extend");
-  const uint32_t T = (uint32_t)sp.search_trees, E = (uint32_t)sp.extend_to, epochs = (uint32_t)sp.epochs;
-  const uint32_t lsize = (uint32_t)sp.init_num * 2 / (5 * T) + 1;  // from the pool size before it grows (:507)
+  const uint32_t T = hs ? 0 : (uint32_t)sp.search_trees, E = (uint32_t)sp.extend_to, epochs = (uint32_t)sp.epochs;
+  const uint32_t lsize = T ? (uint32_t)sp.init_num * 2 / (5 * T) + 1 : 0;  // from the pool size before it grows (:507)
   const uint64_t pool_size = (uint64_t)epochs * E;
   bool sorted = true;
   uint64_t init = (uint64_t)sp.init_num;
@@ -308,6 +314,7 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   kc.o_res = (uint32_t)round_up(kc.o_list + (uint64_t)kc.list_slots * 8, 16);
   kc.o_res2 = (uint32_t)round_up(kc.o_res + (uint64_t)k * 8, 16);
   kc.warp_bytes = (uint32_t)round_up(kc.o_res2 + (uint64_t)k * 8, 16);
+  kc.full_rows = hs ? 1 : 0;
   size_t smem = (size_t)KG_WARPS * kc.warp_bytes;
   if (smem > 200 * 1024) return fail(EFG_ERR_ARG, "kgraph search: k + extend_to too large for shared memory");
 
@@ -322,9 +329,15 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   cfg.seed = idx->bp.seed;
   cfg.nseq = T * lsize;
   uint32_t maxdeg = graph_max_degree(idx);
+  // hash seeds: pool * tables entries per query hold the probe's first `pool` distinct ids
+  const uint64_t cap = hs ? init * hs->tables : 0;
+  if (cap > 0xffffffffull) return fail(EFG_ERR_ARG, "kgraph search: pool * tables too large");
+  cfg.nseeds = (uint32_t)cap;
 
-  const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(nq, (512ull << 20) / (init * 8)));
+  uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(nq, (512ull << 20) / (init * 8)));
+  if (hs) chunk = std::max<uint64_t>(1, std::min<uint64_t>(chunk, (512ull << 20) / (cap * 4)));
   EFG_TRY(idx->kg_keys.reserve(chunk * init));
+  if (hs) EFG_TRY(hs->buf->reserve(chunk * cap));
   EFG_CUDA(cudaFuncSetAttribute(kgraph_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
@@ -346,7 +359,13 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   for (uint64_t q0 = 0; q0 < nq && rc == EFG_OK; q0 += chunk) {
     uint64_t m = std::min(chunk, nq - q0);
     int l = 0;
-    rc = launch_nnexp(idx, cfg, maxdeg, d_q + q0 * qld, m, qld, nullptr, idx->kg_keys.p, s, &l);
+    if (hs) {
+      rc = efg_hash_seeds_device(hs->h, hs->d_qcodes + q0, hs->qstride, m, (uint32_t)cap, hs->buf->p, s);
+      if (rc != EFG_OK) break;
+      ++launches;
+    }
+    rc = launch_nnexp(idx, cfg, maxdeg, d_q + q0 * qld, m, qld, nullptr, idx->kg_keys.p, s, &l, nullptr, nullptr,
+                      hs ? hs->buf->p : nullptr);
     launches += l;
     if (rc == EFG_OK && sorted) {
       rc = launch_row_sort(idx->kg_keys.p, m, (uint32_t)init, (uint32_t)init, s);

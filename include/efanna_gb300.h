@@ -225,14 +225,17 @@ int efg_learned_grad(efg_learned* lr, const float* d_x, uint32_t B, uint64_t row
 int efg_learned_clusters(efg_learned* lr, int32_t* host_assign, uint32_t* host_entries, uint32_t* host_counts);
 void efg_learned_destroy(efg_learned* lr);
 
-/* Hashing-seeded search: the reference's hashing initialiser (HASHINGIndex, search method 1 there:
- * getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp, algorithm/hashing_index.hpp:1087-1200 and
- * 1354-1470).  Every base point has one binary code per hash table (made outside the library, as in
- * the reference; io.read_codes reads its code files).  A query's pool is the first init_num distinct
- * ids met while visiting its Hamming ball of the given radius -- radius by radius, each radius's
- * flipped-bit tuples in ascending lexicographic order, all tables at every mask, bucket members in
- * ascending id order -- topped up by the random fill, then expanded over the graph with the index's
- * search parameters (epochs, init_num, extend_to; no trees are needed).
+/* Hashing-seeded search: the reference's hashing initialiser (HASHINGIndex).  Every base point has
+ * one binary code per hash table (made outside the library, as in the reference; io.read_codes
+ * reads its code files).  A query's pool is the first init_num distinct ids met while visiting its
+ * Hamming ball of the given radius -- radius by radius, each radius's flipped-bit tuples in
+ * ascending lexicographic order, all tables at every mask, bucket members in ascending id order --
+ * topped up by the random fill, then expanded over the graph with the index's search parameters
+ * (epochs, init_num, extend_to; no trees are needed).  The search method follows the hashing
+ * index's numbering (efg_set_search_params' last argument): 1 = pool/extend
+ * (getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp, algorithm/hashing_index.hpp:1087-1200 and
+ * 1354-1470), 0 = kgraph (getNeighborsIEH32_kgraph / _64_kgraph, :1203-1352: the pool size grows
+ * to epochs * extend_to as in the tree-seeded kgraph search, and expansions visit whole graph rows).
  * efg_hash_create: codes = tables x n codes (host, table-major) of code_bits bits (<= 64; the
  * reference's code length after its shift), radius <= min(13, code_bits), Hamming ball x tables <=
  * 2^26 probes.  The tables belong to idx, which must outlive them. */

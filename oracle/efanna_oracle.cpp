@@ -1400,14 +1400,17 @@ static unsigned insert_knn_canon(KPoint* addr, unsigned K, KPoint nn) {
 // One query of getNeighbors_kgraph.  init_num is the pool size in effect for this call (the
 // caller applies the reference's enlargement to epochs * extend_to) and lsize the per-tree leaf
 // count computed from the pool size before that enlargement (:507, :510-514).
+// full_rows: every graph neighbour of an expanded node is visited (the hashing initialiser's
+// kgraph search, hashing_index.hpp:1306-1321) instead of the first extend_to (kdtreeub_index.hpp:599-603).
 static void search_one_kgraph(const Data& X, const Forest& F, const uint64_t* gptr, const uint32_t* gids,
                               const float* q, uint64_t qi, const SearchArgs& a, unsigned lsize, bool sorted,
-                              int mode, uint64_t seed, int32_t* out, uint64_t* nd) {
+                              int mode, uint64_t seed, int32_t* out, uint64_t* nd, bool full_rows = false) {
   size_t N = X.n;
   const unsigned T = (unsigned)a.trees, E = (unsigned)a.extend_to, epochs = (unsigned)a.epochs;
   const unsigned searchK = a.k, pool_size = epochs * E;
   std::vector<uint8_t> flags(N, 0);
-  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, flags);
+  std::vector<int> pool = fill_pool(X, F, q, qi, T, lsize, (unsigned)a.init_num, mode, seed, flags, a.seeds,
+                                    a.nseeds);
   std::vector<std::pair<float, size_t>> result;  // :551-566, in pool order
   for (unsigned j = 0; j < pool.size(); ++j) result.push_back({X.distq(q, X.row(pool[j])), (size_t)pool[j]});
   uint64_t evals = pool.size();
@@ -1440,7 +1443,7 @@ static void search_one_kgraph(const Data& X, const Forest& F, const uint64_t* gp
       if (knn[k].flag) {
         knn[k].flag = false;
         unsigned n = knn[k].id;
-        unsigned maxM = E;
+        unsigned maxM = full_rows ? UINT32_MAX : E;
         unsigned deg = (unsigned)(gptr[n + 1] - gptr[n]);
         if (maxM > deg) maxM = deg;
         for (unsigned m = 0; m < maxM; ++m) {
@@ -1715,11 +1718,42 @@ static void hamming_masks(unsigned bits, unsigned radius, std::vector<uint64_t>&
   }
 }
 
+// Hash tables keyed by the full code (the reference splits it into upper and lower bits for a
+// two-level lookup, BuildHashTable32/64 at hashing_index.hpp:323-346, which finds the same bucket),
+// members in insertion (= id) order; probe() returns a query's first `limit` distinct ids in the
+// visit order of the reference's searches: masks in order, tables inner, bucket members in order.
+struct HashTabs {
+  uint32_t tables;
+  uint64_t n;
+  std::vector<std::unordered_map<uint64_t, std::vector<uint32_t>>> tab;
+  std::vector<uint64_t> masks;
+  HashTabs(const uint64_t* bcodes, uint64_t n_, uint32_t tables_, uint32_t bits, uint32_t radius)
+      : tables(tables_), n(n_), tab(tables_) {
+    for (uint32_t h = 0; h < tables; ++h)
+      for (uint64_t i = 0; i < n; ++i) tab[h][bcodes[(uint64_t)h * n + i]].push_back((uint32_t)i);
+    hamming_masks(bits, radius, masks);
+  }
+  std::vector<uint32_t> probe(const uint64_t* qcodes, uint64_t nq, uint64_t qi, unsigned limit) const {
+    std::vector<uint8_t> seen(n, 0);
+    std::vector<uint32_t> prefix;
+    for (size_t j = 0; j < masks.size() && prefix.size() < limit; ++j)
+      for (uint32_t h = 0; h < tables && prefix.size() < limit; ++h) {
+        auto it = tab[h].find(qcodes[(uint64_t)h * nq + qi] ^ masks[j]);
+        if (it == tab[h].end()) continue;
+        for (size_t e = 0; e < it->second.size() && prefix.size() < limit; ++e) {
+          uint32_t id = it->second[e];
+          if (seen[id]) continue;
+          seen[id] = 1;
+          prefix.push_back(id);
+        }
+      }
+    return prefix;
+  }
+};
+
 // getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp (hashing_index.hpp:1087-1200, 1354-1470):
-// buckets keyed by the full code (the reference splits it into upper and lower bits for a two-level
-// lookup, which finds the same bucket), members in insertion (= id) order; per query, masks in
-// order and tables inner, first occurrences until init_num, then the random fill and the pool /
-// extend expansion of search_one with no trees.  bcodes: tables x n, qcodes: tables x nq.
+// per query the probe's first init_num distinct ids, then the random fill and the pool / extend
+// expansion of search_one with no trees.  bcodes: tables x n, qcodes: tables x nq.
 int orc_search_hashed(const float* data, uint64_t n, uint32_t d, uint64_t ld, const uint64_t* gptr,
                       const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, const uint64_t* bcodes,
                       const uint64_t* qcodes, uint32_t tables, uint32_t bits, uint32_t radius, int epochs,
@@ -1730,11 +1764,7 @@ int orc_search_hashed(const float* data, uint64_t n, uint32_t d, uint64_t ld, co
     return -1;
   if (extend_to > init_num) extend_to = init_num;  // setSearchParams (base_index.hpp:156-157)
   Data X{data, n, d, ld, mode};
-  std::vector<std::unordered_map<uint64_t, std::vector<uint32_t>>> tab(tables);
-  for (uint32_t h = 0; h < tables; ++h)
-    for (uint64_t i = 0; i < n; ++i) tab[h][bcodes[(uint64_t)h * n + i]].push_back((uint32_t)i);
-  std::vector<uint64_t> masks;
-  hamming_masks(bits, radius, masks);
+  HashTabs H(bcodes, n, tables, bits, radius);
   Forest empty;
   if (mode == MODE_SEQ) srand(1);
 #ifdef _OPENMP
@@ -1742,24 +1772,52 @@ int orc_search_hashed(const float* data, uint64_t n, uint32_t d, uint64_t ld, co
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
 #endif
   for (long long i = 0; i < (long long)nq; ++i) {
-    std::vector<uint8_t> seen(n, 0);
-    std::vector<uint32_t> prefix;
-    for (size_t j = 0; j < masks.size() && prefix.size() < (size_t)init_num; ++j)
-      for (uint32_t h = 0; h < tables && prefix.size() < (size_t)init_num; ++h) {
-        auto it = tab[h].find(qcodes[(uint64_t)h * nq + i] ^ masks[j]);
-        if (it == tab[h].end()) continue;
-        for (size_t e = 0; e < it->second.size() && prefix.size() < (size_t)init_num; ++e) {
-          uint32_t id = it->second[e];
-          if (seen[id]) continue;
-          seen[id] = 1;
-          prefix.push_back(id);
-        }
-      }
+    std::vector<uint32_t> prefix = H.probe(qcodes, nq, (uint64_t)i, (unsigned)init_num);
     SearchArgs a{epochs, init_num, extend_to, 0, k};
     a.seeds = prefix.data();
     a.nseeds = (unsigned)prefix.size();
     uint64_t nd = 0;
     search_one(X, empty, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, mode, seed, out + (uint64_t)i * k, &nd);
+    if (evals) evals[i] = nd;
+  }
+  return 0;
+}
+
+// getNeighborsIEH32_kgraph / getNeighborsIEH64_kgraph (hashing_index.hpp:1203-1352 and its 64-bit
+// twin): the pool size is enlarged to epochs * extend_to as in the tree-seeded kgraph search
+// (written back through *init_num), the pool is the probe's first init_num distinct ids plus the
+// random fill, and each expanded node's whole graph row is visited.
+int orc_search_hashed_kgraph(const float* data, uint64_t n, uint32_t d, uint64_t ld, const uint64_t* gptr,
+                             const uint32_t* gids, const float* q, uint64_t nq, uint64_t qld, const uint64_t* bcodes,
+                             const uint64_t* qcodes, uint32_t tables, uint32_t bits, uint32_t radius, int epochs,
+                             int* init_num, int extend_to, uint32_t k, int mode, int threads, uint64_t seed,
+                             int32_t* out, uint64_t* evals) {
+  if (tables < 1 || bits < 1 || bits > 64 || !init_num || *init_num <= 0 || k == 0 || epochs < 0 || extend_to < 0)
+    return -1;
+  if (extend_to > *init_num) extend_to = *init_num;  // setSearchParams (base_index.hpp:156-157)
+  unsigned pool_size = (unsigned)epochs * (unsigned)extend_to;
+  bool sorted = true;
+  if (pool_size >= (unsigned)*init_num) {  // :1212-1216
+    *init_num = (int)pool_size;
+    sorted = false;
+  }
+  if ((uint64_t)*init_num > n || *init_num <= 0) return -1;  // the random fill would not end
+  Data X{data, n, d, ld, mode};
+  HashTabs H(bcodes, n, tables, bits, radius);
+  Forest empty;
+  if (mode == MODE_SEQ) srand(1);
+#ifdef _OPENMP
+  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+#endif
+  for (long long i = 0; i < (long long)nq; ++i) {
+    std::vector<uint32_t> prefix = H.probe(qcodes, nq, (uint64_t)i, (unsigned)*init_num);
+    SearchArgs a{epochs, *init_num, extend_to, 0, k};
+    a.seeds = prefix.data();
+    a.nseeds = (unsigned)prefix.size();
+    uint64_t nd = 0;
+    search_one_kgraph(X, empty, gptr, gids, q + (uint64_t)i * qld, (uint64_t)i, a, 0, sorted, mode, seed,
+                      out + (uint64_t)i * k, &nd, true);
     if (evals) evals[i] = nd;
   }
   return 0;

@@ -89,6 +89,10 @@ def lib():
         L.orc_search_hashed.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, u64p, u32p, f32p, C.c_uint64,
                                         C.c_uint64, u64p, u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int,
                                         C.c_int, C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p, u64p]
+        L.orc_search_hashed_kgraph.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, u64p, u32p, f32p,
+                                               C.c_uint64, C.c_uint64, u64p, u64p, C.c_uint32, C.c_uint32,
+                                               C.c_uint32, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_uint32, C.c_int,
+                                               C.c_int, C.c_uint64, i32p, u64p]
         _lib = L
     return _lib
 
@@ -300,3 +304,28 @@ def search_hashed(data, gptr, gids, queries, bcodes, qcodes, bits, radius, k=10,
     if rc != 0:
         raise ValueError("orc_search_hashed rejected its arguments")
     return out, ev
+
+
+def search_hashed_kgraph(data, gptr, gids, queries, bcodes, qcodes, bits, radius, k=10, epochs=4, init_num=1200,
+                         extend_to=200, mode: int = CANON, threads: int = 1, seed: int = 1998):
+    """getNeighborsIEH32_kgraph / getNeighborsIEH64_kgraph.  Returns (ids, evals per query, pool
+    size in effect afterwards)."""
+    data = np.ascontiguousarray(data, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    gptr = np.ascontiguousarray(gptr, np.uint64)
+    gids = np.ascontiguousarray(gids, np.uint32)
+    bcodes = np.ascontiguousarray(bcodes, np.uint64)
+    qcodes = np.ascontiguousarray(qcodes, np.uint64)
+    nq = queries.shape[0]
+    assert bcodes.shape == (qcodes.shape[0], data.shape[0]) and qcodes.shape[1] == nq
+    out = np.zeros((nq, k), np.int32)
+    ev = np.zeros(nq, np.uint64)
+    pool = C.c_int(init_num)
+    rc = lib().orc_search_hashed_kgraph(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1],
+                                        _p(gptr, C.c_uint64), _p(gids, C.c_uint32), _p(queries, C.c_float), nq,
+                                        queries.shape[1], _p(bcodes, C.c_uint64), _p(qcodes, C.c_uint64),
+                                        bcodes.shape[0], bits, radius, epochs, C.byref(pool), extend_to, k, mode,
+                                        threads, seed, _p(out, C.c_int32), _p(ev, C.c_uint64))
+    if rc != 0:
+        raise ValueError("orc_search_hashed_kgraph rejected its arguments")
+    return out, ev, pool.value

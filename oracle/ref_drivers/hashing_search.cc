@@ -1,11 +1,12 @@
-// Test infrastructure only: a driver that runs the reference's hashing-seeded pool/extend search
-// (HASHINGIndex, search method 1: getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp), which has no
-// sample program in the reference tree.  Compiled against the reference's headers by
+// Test infrastructure only: a driver that runs the reference's hashing-seeded searches (HASHINGIndex,
+// search method 1: getNeighborsIEH32_nnexp / getNeighborsIEH64_nnexp; method 0: the kgraph search
+// getNeighborsIEH32_kgraph / getNeighborsIEH64_kgraph), which have no sample program in the
+// reference tree.  Compiled against the reference's headers by
 // `make -C oracle ref`; it goes through the public FIndex API as a C++ user of the reference would:
 // HASHINGIndexParams, buildIndex (the hash tables), loadGraph, setSearchParams, knnSearch.
 //
 //   hashing_search data.fvecs graph queries.fvecs base_codes query_codes results.ivecs
-//                  codelen tables upbits radius shift epochs pool extend k
+//                  codelen tables upbits radius shift epochs pool extend k [method]
 //
 // base_codes / query_codes are code-file prefixes (files <prefix>_1 ... <prefix>_<tables>).
 #include <malloc.h>
@@ -45,10 +46,10 @@ static float* read_fvecs_padded(const char* path, size_t& n, int& dim) {
 }
 
 int main(int argc, char** argv) {
-  if (argc != 16) {
+  if (argc != 16 && argc != 17) {
     std::cerr << "usage: " << argv[0]
               << " data graph queries base_codes query_codes results codelen tables upbits radius shift"
-                 " epochs pool extend k\n";
+                 " epochs pool extend k [method]\n";
     return 1;
   }
   size_t n = 0, nq = 0;
@@ -64,7 +65,8 @@ int main(int argc, char** argv) {
                                          std::atoi(argv[10]), bcf, qcf, std::atoi(argv[11])));
   index.buildIndex();
   index.loadGraph(argv[2]);
-  index.setSearchParams(std::atoi(argv[12]), std::atoi(argv[13]), std::atoi(argv[14]), 0, -1, 1);
+  index.setSearchParams(std::atoi(argv[12]), std::atoi(argv[13]), std::atoi(argv[14]), 0, -1,
+                        argc == 17 ? std::atoi(argv[16]) : 1);
   index.knnSearch(std::atoi(argv[15]), queries);
   index.saveResults(argv[6]);
   return 0;

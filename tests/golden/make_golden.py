@@ -19,7 +19,8 @@ across runs) on small seeded integer-valued data, and stores inputs and outputs:
                its FIndex API via oracle/ref_drivers/hashing_search.cc) on the case's graph file with
                seeded sign-of-projection codes (datasets.sign_codes) written as the reference's code
                files, for each parameter set in HASH_POINTS: the codes as read back (tables x n and
-               tables x nq, after the shift), the code length in effect and the ids.
+               tables x nq, after the shift), the code length in effect and the ids; the same for
+               its kgraph search (search method 0 there) as kgraph_<i>.
 
 ``--only-kgraph`` / ``--only-hashing`` regenerate just those fixtures.
 
@@ -116,8 +117,11 @@ def make_hashing(name, tmp):
     for i, (clen, tables, up, rad, shift, ep, pool, ext, k) in enumerate(HASH_POINTS):
         io.write_codes(bpre, datasets.sign_codes(x, tables, clen, seed=100 + i), clen)
         io.write_codes(qpre, datasets.sign_codes(q, tables, clen, seed=100 + i, center=x.mean(0)), clen)
-        run([O.ref_bin("hashing_search", "strict"), base, os.path.join(HERE, name + ".graph"), qf, bpre, qpre, r,
-             str(clen), str(tables), str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k)], 1)
+        args = [O.ref_bin("hashing_search", "strict"), base, os.path.join(HERE, name + ".graph"), qf, bpre, qpre, r,
+                str(clen), str(tables), str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k)]
+        run(args + ["0"], 1)
+        out["kgraph_%d" % i] = io.read_ivecs(r)
+        run(args, 1)
         bc, bits = io.read_codes(bpre, tables, clen, shift)
         qc, _ = io.read_codes(qpre, tables, clen, shift)
         word = np.uint32 if bits <= 32 else np.uint64

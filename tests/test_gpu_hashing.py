@@ -1,7 +1,8 @@
-"""Hashing-seeded search on the GPU (the reference's HASHINGIndex with its pool/extend search,
-algorithm/hashing_index.hpp:1087-1200): the probe sequence against a plain-Python restatement of
-the reference's bucket visits, and the search against the oracle's canonical mode -- over the
-golden fixture's code sets (made by the reference's own code-file reader) and larger Hamming balls."""
+"""Hashing-seeded searches on the GPU (the reference's HASHINGIndex: pool/extend search,
+algorithm/hashing_index.hpp:1087-1200, and kgraph search, :1203-1352): the probe sequence against a
+plain-Python restatement of the reference's bucket visits, and both searches against the oracle's
+canonical mode -- over the golden fixture's code sets (read back the way the reference reads its
+code files) and larger Hamming balls."""
 import itertools
 import os
 
@@ -72,7 +73,7 @@ def test_search_matches_oracle_on_reference_code_sets(efg, oracle_lib, case):
         clen, tables, up, rad, shift, ep, pool, ext, k = [int(v) for v in pt]
         bc, qc, bits = hz["bcodes_%d" % i].astype(np.uint64), hz["qcodes_%d" % i].astype(np.uint64), int(hz["bits_%d" % i])
         ht = efg.HashTables(idx, bc, bits, rad)
-        idx.set_search_params(ep, pool, ext, 1)
+        idx.set_search_params(ep, pool, ext, 1, -1, 1)
         res = ht.search(k, q, qc)
         ref, _ = O.search_hashed(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool, extend_to=ext,
                                  mode=O.CANON, threads=4)
@@ -96,11 +97,37 @@ def test_search_matches_oracle_larger_balls(efg, oracle_lib, case, bits, tables,
     bc = datasets.sign_codes(x, tables, bits, seed=bits)
     qc = datasets.sign_codes(q, tables, bits, seed=bits, center=x.mean(0))
     ht = efg.HashTables(idx, bc, bits, radius)
-    idx.set_search_params(3, pool, 50, 1)
+    idx.set_search_params(3, pool, 50, 1, -1, 1)
     res = ht.search(10, q, qc)
     ref, _ = O.search_hashed(x, gp, gi, q, bc, qc, bits, radius, k=10, epochs=3, init_num=pool, extend_to=50,
                              mode=O.CANON, threads=4)
     assert np.array_equal(res, ref)
+    ht.close()
+
+
+def test_kgraph_search_matches_oracle(efg, oracle_lib, case):
+    """The hashing index's kgraph search (method 0 there): pools from the probe sequence, whole
+    graph rows per expansion, the stored pool size raised to epochs * extend_to."""
+    O = oracle_lib
+    idx, x, q, gp, gi, hz = case
+    for i, pt in enumerate(hz["points"]):
+        clen, tables, up, rad, shift, ep, pool, ext, k = [int(v) for v in pt]
+        bc, qc, bits = hz["bcodes_%d" % i].astype(np.uint64), hz["qcodes_%d" % i].astype(np.uint64), int(hz["bits_%d" % i])
+        ht = efg.HashTables(idx, bc, bits, rad)
+        idx.set_search_params(ep, pool, ext, 1, -1, 0)
+        res = ht.search(k, q, qc)
+        ref, _, _ = O.search_hashed_kgraph(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool,
+                                           extend_to=ext, mode=O.CANON, threads=4)
+        assert np.array_equal(res, ref), i
+        ht.close()
+    # a 64-bit code set with a deeper ball
+    bc = datasets.sign_codes(x, 2, 48, seed=9)
+    qc = datasets.sign_codes(q, 2, 48, seed=9, center=x.mean(0))
+    ht = efg.HashTables(idx, bc, 48, 2)
+    idx.set_search_params(4, 300, 60, 1, -1, 0)
+    ref, _, _ = O.search_hashed_kgraph(x, gp, gi, q, bc, qc, 48, 2, k=10, epochs=4, init_num=300, extend_to=60,
+                                       mode=O.CANON, threads=4)
+    assert np.array_equal(ht.search(10, q, qc), ref)
     ht.close()
 
 
@@ -114,7 +141,7 @@ def test_hash_argument_errors(efg, case):
     with pytest.raises(efg.EfannaError):
         efg.HashTables(idx, datasets.sign_codes(x, 2, 64, seed=1), 64, 6)  # ball of ~7.6e7 masks x 2 tables
     ht = efg.HashTables(idx, bc, 16, 1)
-    idx.set_search_params(3, 200, 40, 1)
+    idx.set_search_params(3, 200, 40, 1, -1, 1)
     with pytest.raises(efg.EfannaError):
         ht.search(201, q, datasets.sign_codes(q, 2, 16, seed=1))  # k above the pool
     assert ht.search(10, q[:0], np.zeros((2, 0), np.uint64)).shape == (0, 10)
@@ -133,7 +160,7 @@ def test_reference_api_program_through_facade(efg, oracle_lib, case, tmp_path):
     bf, qf, rf = str(tmp_path / "b.fvecs"), str(tmp_path / "q.fvecs"), str(tmp_path / "r.ivecs")
     io.write_fvecs(bf, x)
     io.write_fvecs(qf, q)
-    for i in (0, 1, 2):
+    for i, method in ((0, 1), (1, 1), (2, 1), (0, 0), (2, 0)):
         clen, tables, up, rad, shift, ep, pool, ext, k = [int(v) for v in hz["points"][i]]
         bc, qc, bits = hz["bcodes_%d" % i].astype(np.uint64), hz["qcodes_%d" % i].astype(np.uint64), int(hz["bits_%d" % i])
         # the files hold the codes before the shift (any low bits: the reader drops them)
@@ -141,8 +168,12 @@ def test_reference_api_program_through_facade(efg, oracle_lib, case, tmp_path):
         io.write_codes(str(tmp_path / "qc"), qc << np.uint64(shift), clen)
         r = subprocess.run([exe, bf, os.path.join(GOLDEN, "small_d32.graph"), qf, str(tmp_path / "bc"),
                             str(tmp_path / "qc"), rf, str(clen), str(tables), str(up), str(rad), str(shift), str(ep),
-                            str(pool), str(ext), str(k)], capture_output=True, text=True)
+                            str(pool), str(ext), str(k), str(method)], capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
-        ref, _ = O.search_hashed(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool, extend_to=ext,
-                                 mode=O.CANON, threads=4)
-        assert np.array_equal(io.read_ivecs(rf), ref), i
+        if method == 1:
+            ref, _ = O.search_hashed(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool, extend_to=ext,
+                                     mode=O.CANON, threads=4)
+        else:
+            ref, _, _ = O.search_hashed_kgraph(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool,
+                                               extend_to=ext, mode=O.CANON, threads=4)
+        assert np.array_equal(io.read_ivecs(rf), ref), (i, method)

@@ -201,3 +201,17 @@ def test_hashing_canonical_close_to_reference(oracle_lib):
         assert abs(recall(out) - recall(ref)) < 0.03, i
         if i != 1:
             assert same_sets > 0.97, (i, same_sets)
+
+
+def test_hashing_kgraph_seq_matches_reference_results(oracle_lib):
+    """getNeighborsIEH32_kgraph / IEH64_kgraph restated (whole graph rows per expansion, the pool
+    size raised to epochs * extend_to where that is not smaller): byte-identical ids to the
+    reference's hashing kgraph search (search method 0 there)."""
+    O = oracle_lib
+    x, q, hz, gp, gi = _hashing_case()
+    for i, (clen, tables, up, rad, shift, ep, pool, ext, k) in enumerate(hz["points"]):
+        out, _, pool2 = O.search_hashed_kgraph(x, gp, gi, q, hz["bcodes_%d" % i], hz["qcodes_%d" % i],
+                                               int(hz["bits_%d" % i]), int(rad), k=int(k), epochs=int(ep),
+                                               init_num=int(pool), extend_to=int(ext), mode=O.SEQ)
+        assert np.array_equal(out, hz["kgraph_%d" % i]), i
+        assert pool2 == max(int(pool), int(ep) * min(int(ext), int(pool)))

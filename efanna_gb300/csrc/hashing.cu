@@ -15,7 +15,9 @@
 //     and copies the buckets it hits, in probe order, into the query's seed row; a row of
 //     pool * tables entries always holds the first `pool` distinct ids of the probe sequence (each
 //     id sits in one bucket per table), and the search kernel keeps first occurrences;
-//   * the pool/extend kernel with seeds and no trees (search_device_ex with use_trees = false).
+//   * the pool/extend kernel with seeds and no trees (search_device_ex with use_trees = false);
+//     without a graph, the same kernel with no epochs ranks the bucket ids, the random fill topping
+//     the pool up to k only (the graph-less search getNeighbors32 / getNeighbors64, :929-1085).
 #include <algorithm>
 #include <vector>
 
@@ -261,11 +263,12 @@ int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64
   if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   if (qcode_stride < nq) return fail(EFG_ERR_ARG, "qcode_stride < nq");
   const SearchParams& sp = idx->sp;
-  if (sp.method == 0) {  // the hashing initialiser's kgraph search (its method 0)
+  const bool buckets_only = !idx->graph.valid;  // getNeighbors32 / getNeighbors64 (:929-1085)
+  if (!buckets_only && sp.method == 0) {  // the hashing initialiser's kgraph search (its method 0)
     KgSeedSource src{h, d_qcodes, qcode_stride, h->tables, &h->seeds};
     return kgraph_search_device(idx, d_q, nq, row_stride, k, d_out, (cudaStream_t)stream, false, &src);
   }
-  if (sp.method != 1) return fail(EFG_ERR_ARG, "no such searching method");
+  if (!buckets_only && sp.method != 1) return fail(EFG_ERR_ARG, "no such searching method");
   if (sp.init_num <= 0 || (uint64_t)sp.init_num > idx->n) return fail(EFG_ERR_ARG, "pool size must be in [1, n]");
   if (nq == 0) return EFG_OK;
   efg_query_params lim{sp.epochs, sp.init_num, sp.extend_to, k};
@@ -277,7 +280,7 @@ int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64
     const uint64_t m = std::min(chunk, nq - q0);
     EFG_TRY(efg_hash_seeds_device(h, d_qcodes + q0, qcode_stride, m, cap_q, h->seeds.p, s));
     EFG_TRY(search_device_ex(idx, d_q + q0 * row_stride, m, row_stride, lim, nullptr, nullptr, d_out + q0 * k, s,
-                             false, h->seeds.p, cap_q, false));
+                             false, h->seeds.p, cap_q, false, buckets_only));
   }
   return EFG_OK;
 }

@@ -140,7 +140,7 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
                      bool count_evals, const uint32_t* d_seeds = nullptr, uint32_t seeds_per_query = 0,
-                     bool use_trees = true);
+                     bool use_trees = true, bool bucket_only = false);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
 // Builds the FP8 e4m3 screening copy of the base with one FP32 scale per row.

@@ -380,12 +380,20 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
   return EFG_OK;
 }
 
-int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
+int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim_in,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
-                     bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query, bool use_trees) {
+                     bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query, bool use_trees,
+                     bool bucket_only) {
   const SearchParams& sp = idx->sp;
+  efg_query_params lim = lim_in;
   const uint32_t k = lim.k;
-  if (use_trees) {
+  if (bucket_only) {  // the seeds ranked, topped up to k: no trees, no graph, no epochs
+    if (!d_seeds && nq) return fail(EFG_ERR_ARG, "the bucket search needs seeds");
+    if (k == 0) return fail(EFG_ERR_ARG, "k must be positive");
+    use_trees = false;
+    lim.epochs = 0;
+    lim.extend_to = 0;
+  } else if (use_trees) {
     EFG_TRY(search_common_checks(idx, k));
   } else {  // a pool from the seeds alone (then the random fill): no trees needed
     if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");
@@ -407,6 +415,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
   cfg.nseeds = d_seeds ? seeds_per_query : 0;
+  cfg.fill_k = bucket_only ? 1 : 0;
   if (idx->precision == EFG_PRECISION_FP8) {
     if (!idx->base8.p) EFG_TRY(make_base8(idx));
     cfg.fp8 = 1;

@@ -31,6 +31,7 @@ struct SearchCfg {
   uint32_t fixed_k;     // graph degree when every row has it (0: row pointers), and
   uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices
   uint32_t nseeds;      // entry seeds per query placed ahead of the leaves (learned form)
+  uint32_t fill_k;      // 1: the random fill tops the pool up to k only (the graph-less bucket search)
   uint64_t seed;
 };
 

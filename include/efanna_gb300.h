@@ -250,7 +250,9 @@ uint64_t efg_hash_ball_size(const efg_hash* h);
  * distinct ids. */
 int efg_hash_seeds_device(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_stride, uint64_t nq,
                           uint32_t seeds_per_query, uint32_t* d_seeds, void* stream);
-/* The hashing-seeded search over device queries and codes: nq rows of k ids into d_out. */
+/* The hashing-seeded search over device queries and codes: nq rows of k ids into d_out.  Without a
+ * graph on the index it is the reference's graph-less bucket search (getNeighbors32 / _64,
+ * :929-1085): the pool's bucket ids, topped up by the random fill to k only, ranked by distance. */
 int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_queries, uint64_t nq, uint64_t row_stride,
                            const uint64_t* d_qcodes, uint64_t qcode_stride, uint32_t k, int32_t* d_out_ids,
                            void* stream);

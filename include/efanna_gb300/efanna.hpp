@@ -10,9 +10,9 @@
 //                         general/params.hpp:7-42
 //   KDTreeUbIndexParams   algorithm/kdtreeub_index.hpp:14-35
 //   HASHINGIndexParams    algorithm/hashing_index.hpp:19-46 (the hashing initialiser: its code
-//                         files, hash tables and the two searches seeded from them over a loaded
-//                         graph -- method 1 pool/extend, method 0 kgraph; its graph-less bucket
-//                         search is not provided and throws)
+//                         files, hash tables and the searches seeded from them: over a loaded
+//                         graph method 1 pool/extend and method 0 kgraph, without a graph the
+//                         bucket search)
 //   Matrix                general/matrix.hpp:12-72
 //   Distance, L2Distance, L2DistanceSSE, L2DistanceAVX, L2DistanceAVXr4
 //                         general/distance.hpp:46-379 (here plain C++; the GPU computes the
@@ -391,9 +391,7 @@ class FIndex {
     return all;
   }
   void hashing_search(int k, const Matrix<DataType>& query) {
-    if (efg_graph_size(idx_) == 0)
-      throw std::runtime_error("efanna_gb300 provides the hashing initialiser's searches over a loaded graph only");
-    if (method_ != 0 && method_ != 1) {
+    if (efg_graph_size(idx_) != 0 && method_ != 0 && method_ != 1) {
       std::cout << "no such searching method" << std::endl;
       return;
     }

@@ -1823,6 +1823,45 @@ int orc_search_hashed_kgraph(const float* data, uint64_t n, uint32_t d, uint64_t
   return 0;
 }
 
+// getNeighbors32 / getNeighbors64 (hashing_index.hpp:929-1085, the hashing index without a graph):
+// the probe's first init_num distinct ids, topped up by the random fill to k only when fewer, ranked
+// by (distance, id) (partial_sort of (dist, id) pairs); the first k ids.
+int orc_search_hashed_buckets(const float* data, uint64_t n, uint32_t d, uint64_t ld, const float* q, uint64_t nq,
+                              uint64_t qld, const uint64_t* bcodes, const uint64_t* qcodes, uint32_t tables,
+                              uint32_t bits, uint32_t radius, int init_num, uint32_t k, int mode, int threads,
+                              uint64_t seed, int32_t* out) {
+  if (tables < 1 || bits < 1 || bits > 64 || init_num <= 0 || k == 0 || k > (uint32_t)init_num ||
+      (uint64_t)k > n)
+    return -1;
+  Data X{data, n, d, ld, mode};
+  HashTabs H(bcodes, n, tables, bits, radius);
+  if (mode == MODE_SEQ) srand(1);
+#ifdef _OPENMP
+  int nt = (mode == MODE_SEQ || threads < 1) ? 1 : threads;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+#endif
+  for (long long i = 0; i < (long long)nq; ++i) {
+    std::vector<uint32_t> pool = H.probe(qcodes, nq, (uint64_t)i, (unsigned)init_num);
+    if (pool.size() < k) {  // :976-985
+      std::vector<uint8_t> seen(n, 0);
+      for (uint32_t id : pool) seen[id] = 1;
+      CRng g(hash4(seed, TAG_SFILL, (uint64_t)i, 0, 0));
+      while (pool.size() < k) {
+        uint32_t id = mode == MODE_SEQ ? (uint32_t)(rand() % (int)n) : g.next() % (uint32_t)n;
+        if (seen[id]) continue;
+        seen[id] = 1;
+        pool.push_back(id);
+      }
+    }
+    const float* qr = q + (uint64_t)i * qld;
+    std::vector<std::pair<float, size_t>> result;
+    for (uint32_t id : pool) result.push_back({X.distq(qr, X.row(id)), (size_t)id});
+    std::partial_sort(result.begin(), result.begin() + k, result.end());
+    for (uint32_t j = 0; j < k; ++j) out[(uint64_t)i * k + j] = (int32_t)result[j].second;
+  }
+  return 0;
+}
+
 // Batched kgraph search (getNeighbors_kgraph).  *init_num is the index's pool size; like the
 // reference (kdtreeub_index.hpp:510-514) it is raised to epochs * extend_to when that is not
 // smaller, and the raised value is written back for the caller's next search.

@@ -93,6 +93,9 @@ def lib():
                                                C.c_uint64, C.c_uint64, u64p, u64p, C.c_uint32, C.c_uint32,
                                                C.c_uint32, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_uint32, C.c_int,
                                                C.c_int, C.c_uint64, i32p, u64p]
+        L.orc_search_hashed_buckets.argtypes = [f32p, C.c_uint64, C.c_uint32, C.c_uint64, f32p, C.c_uint64,
+                                                C.c_uint64, u64p, u64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int,
+                                                C.c_uint32, C.c_int, C.c_int, C.c_uint64, i32p]
         _lib = L
     return _lib
 
@@ -329,3 +332,21 @@ def search_hashed_kgraph(data, gptr, gids, queries, bcodes, qcodes, bits, radius
     if rc != 0:
         raise ValueError("orc_search_hashed_kgraph rejected its arguments")
     return out, ev, pool.value
+
+
+def search_hashed_buckets(data, queries, bcodes, qcodes, bits, radius, k=10, init_num=1200, mode: int = CANON,
+                          threads: int = 1, seed: int = 1998):
+    """getNeighbors32 / getNeighbors64: the hashing index's search without a graph."""
+    data = np.ascontiguousarray(data, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    bcodes = np.ascontiguousarray(bcodes, np.uint64)
+    qcodes = np.ascontiguousarray(qcodes, np.uint64)
+    nq = queries.shape[0]
+    out = np.zeros((nq, k), np.int32)
+    rc = lib().orc_search_hashed_buckets(_p(data, C.c_float), data.shape[0], data.shape[1], data.shape[1],
+                                         _p(queries, C.c_float), nq, queries.shape[1], _p(bcodes, C.c_uint64),
+                                         _p(qcodes, C.c_uint64), bcodes.shape[0], bits, radius, init_num, k, mode,
+                                         threads, seed, _p(out, C.c_int32))
+    if rc != 0:
+        raise ValueError("orc_search_hashed_buckets rejected its arguments")
+    return out

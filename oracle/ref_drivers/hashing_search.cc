@@ -8,7 +8,8 @@
 //   hashing_search data.fvecs graph queries.fvecs base_codes query_codes results.ivecs
 //                  codelen tables upbits radius shift epochs pool extend k [method]
 //
-// base_codes / query_codes are code-file prefixes (files <prefix>_1 ... <prefix>_<tables>).
+// base_codes / query_codes are code-file prefixes (files <prefix>_1 ... <prefix>_<tables>).  A graph
+// argument of "-" loads no graph: the index then runs its graph-less bucket search (getNeighbors32).
 #include <malloc.h>
 
 #include <cstdlib>
@@ -64,7 +65,7 @@ int main(int argc, char** argv) {
                       HASHINGIndexParams(std::atoi(argv[7]), std::atoi(argv[8]), std::atoi(argv[9]),
                                          std::atoi(argv[10]), bcf, qcf, std::atoi(argv[11])));
   index.buildIndex();
-  index.loadGraph(argv[2]);
+  if (std::strcmp(argv[2], "-") != 0) index.loadGraph(argv[2]);
   index.setSearchParams(std::atoi(argv[12]), std::atoi(argv[13]), std::atoi(argv[14]), 0, -1,
                         argc == 17 ? std::atoi(argv[16]) : 1);
   index.knnSearch(std::atoi(argv[15]), queries);

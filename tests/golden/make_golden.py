@@ -20,7 +20,8 @@ across runs) on small seeded integer-valued data, and stores inputs and outputs:
                seeded sign-of-projection codes (datasets.sign_codes) written as the reference's code
                files, for each parameter set in HASH_POINTS: the codes as read back (tables x n and
                tables x nq, after the shift), the code length in effect and the ids; the same for
-               its kgraph search (search method 0 there) as kgraph_<i>.
+               its kgraph search (search method 0 there) as kgraph_<i> and for its search without
+               a graph (the bucket search) as buckets_<i>.
 
 ``--only-kgraph`` / ``--only-hashing`` regenerate just those fixtures.
 
@@ -121,6 +122,8 @@ def make_hashing(name, tmp):
                 str(clen), str(tables), str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k)]
         run(args + ["0"], 1)
         out["kgraph_%d" % i] = io.read_ivecs(r)
+        run(args[:2] + ["-"] + args[3:], 1)
+        out["buckets_%d" % i] = io.read_ivecs(r)
         run(args, 1)
         bc, bits = io.read_codes(bpre, tables, clen, shift)
         qc, _ = io.read_codes(qpre, tables, clen, shift)

@@ -131,6 +131,23 @@ def test_kgraph_search_matches_oracle(efg, oracle_lib, case):
     ht.close()
 
 
+def test_bucket_search_without_graph_matches_oracle(efg, oracle_lib, case):
+    """The hashing index without a graph (getNeighbors32 / _64): bucket ids ranked, the random fill
+    only up to k."""
+    O = oracle_lib
+    _, x, q, _, _, hz = case
+    idx = efg.Index(x, efg.IndexParams())
+    for i, pt in enumerate(hz["points"]):
+        clen, tables, up, rad, shift, ep, pool, ext, k = [int(v) for v in pt]
+        bc, qc, bits = hz["bcodes_%d" % i].astype(np.uint64), hz["qcodes_%d" % i].astype(np.uint64), int(hz["bits_%d" % i])
+        ht = efg.HashTables(idx, bc, bits, rad)
+        idx.set_search_params(ep, pool, ext, 1, -1, 1)
+        ref = O.search_hashed_buckets(x, q, bc, qc, bits, rad, k=k, init_num=pool, mode=O.CANON, threads=4)
+        assert np.array_equal(ht.search(k, q, qc), ref), i
+        ht.close()
+    idx.close()
+
+
 def test_hash_argument_errors(efg, case):
     idx, x, q, *_ = case
     bc = datasets.sign_codes(x, 2, 16, seed=1)
@@ -160,17 +177,20 @@ def test_reference_api_program_through_facade(efg, oracle_lib, case, tmp_path):
     bf, qf, rf = str(tmp_path / "b.fvecs"), str(tmp_path / "q.fvecs"), str(tmp_path / "r.ivecs")
     io.write_fvecs(bf, x)
     io.write_fvecs(qf, q)
-    for i, method in ((0, 1), (1, 1), (2, 1), (0, 0), (2, 0)):
+    for i, method in ((0, 1), (1, 1), (2, 1), (0, 0), (2, 0), (0, -1), (3, -1)):  # -1: no graph
         clen, tables, up, rad, shift, ep, pool, ext, k = [int(v) for v in hz["points"][i]]
         bc, qc, bits = hz["bcodes_%d" % i].astype(np.uint64), hz["qcodes_%d" % i].astype(np.uint64), int(hz["bits_%d" % i])
         # the files hold the codes before the shift (any low bits: the reader drops them)
         io.write_codes(str(tmp_path / "bc"), bc << np.uint64(shift), clen)
         io.write_codes(str(tmp_path / "qc"), qc << np.uint64(shift), clen)
-        r = subprocess.run([exe, bf, os.path.join(GOLDEN, "small_d32.graph"), qf, str(tmp_path / "bc"),
-                            str(tmp_path / "qc"), rf, str(clen), str(tables), str(up), str(rad), str(shift), str(ep),
-                            str(pool), str(ext), str(k), str(method)], capture_output=True, text=True)
+        graph = os.path.join(GOLDEN, "small_d32.graph") if method >= 0 else "-"
+        r = subprocess.run([exe, bf, graph, qf, str(tmp_path / "bc"), str(tmp_path / "qc"), rf, str(clen), str(tables),
+                            str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k), str(method if method >= 0 else 1)],
+                           capture_output=True, text=True)
         assert r.returncode == 0, r.stdout + r.stderr
-        if method == 1:
+        if method < 0:
+            ref = O.search_hashed_buckets(x, q, bc, qc, bits, rad, k=k, init_num=pool, mode=O.CANON, threads=4)
+        elif method == 1:
             ref, _ = O.search_hashed(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool, extend_to=ext,
                                      mode=O.CANON, threads=4)
         else:

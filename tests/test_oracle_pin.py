@@ -215,3 +215,14 @@ def test_hashing_kgraph_seq_matches_reference_results(oracle_lib):
                                                init_num=int(pool), extend_to=int(ext), mode=O.SEQ)
         assert np.array_equal(out, hz["kgraph_%d" % i]), i
         assert pool2 == max(int(pool), int(ep) * min(int(ext), int(pool)))
+
+
+def test_hashing_bucket_search_seq_matches_reference_results(oracle_lib):
+    """getNeighbors32 / getNeighbors64 restated (the hashing index without a graph: bucket ids,
+    random fill to k only, ranked): byte-identical ids to the reference's."""
+    O = oracle_lib
+    x, q, hz, gp, gi = _hashing_case()
+    for i, (clen, tables, up, rad, shift, ep, pool, ext, k) in enumerate(hz["points"]):
+        out = O.search_hashed_buckets(x, q, hz["bcodes_%d" % i], hz["qcodes_%d" % i], int(hz["bits_%d" % i]),
+                                      int(rad), k=int(k), init_num=int(pool), mode=O.SEQ)
+        assert np.array_equal(out, hz["buckets_%d" % i]), i

@@ -37,8 +37,15 @@ METRIC = "graph build s & QPS at recall@10>=0.95, 1xGB300: plain FP32 vs BF16+le
 GRAPH = dict(trees=8, merge_level=8, epochs=8, check=25, L=30, K=10, S=10)
 SEARCH_TREES = 16
 CONFIG_POINT = (4, 1200, 200)  # the reference configuration's epochs / pool / extend
-LADDER = [(4, 1200, 200), (4, 2400, 400), (6, 4000, 400), (6, 4000, 600), (8, 6000, 600), (8, 8000, 800),
-          (8, 12000, 1200), (12, 16000, 1600)]
+# search settings (epochs, pool, extend) in ascending cost; the first reaching the target recall is
+# the operating point.  Index 4 is where the plain FP32 search with 16 trees reaches it on this
+# workload (the reference arm runs there).
+LADDER = [(4, 1200, 200), (4, 2400, 400), (4, 3000, 600), (4, 3500, 700), (4, 4000, 750), (4, 5000, 800),
+          (6, 6000, 800), (8, 8000, 1000), (8, 12000, 1200), (12, 16000, 1600)]
+# the same search over 48 trees (more, smaller leaf lists for the same pool): a setting beside the
+# configuration's 16 trees
+WIDE_TREES = 48
+WIDE_LADDER = [(5, 2500, 500), (5, 3000, 600), (5, 3500, 700), (6, 4000, 800), (8, 6000, 800), (8, 8000, 1000)]
 TARGET = 0.95
 
 
@@ -157,17 +164,17 @@ def run_gpu(args):
     out = torch.zeros((nq, 10), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream()
 
-    def search_once(point):
-        idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
+    def search_once(point, trees=SEARCH_TREES):
+        idx.set_search_params(point[0], point[1], point[2], trees)
         idx.knn_search_device(10, Q.data_ptr(), nq, 128, out.data_ptr(), stream.cuda_stream)
 
-    def measure(precision):
+    def measure(precision, trees=SEARCH_TREES, points=LADDER):
         """Operating point, device-timed QPS, e2e QPS and roofline inputs for one search precision."""
         idx.set_search_precision(precision)
         ladder, point = [], None
-        for pt in LADDER:  # first ladder entry reaching the target recall
+        for pt in points:  # first ladder entry reaching the target recall
             try:
-                search_once(pt)
+                search_once(pt, trees)
                 torch.cuda.synchronize()
             except E.EfannaError as e:
                 log("skip", pt, e)
@@ -178,12 +185,12 @@ def run_gpu(args):
                 point = pt
                 break
         if point is None:
-            point = LADDER[-1]
-        search_once(CONFIG_POINT)
+            point = points[-1]
+        search_once(CONFIG_POINT, trees)
         torch.cuda.synchronize()
         res_cfg = recall(out.cpu().numpy(), gt)
         # evals / expansions / launches at the operating point (the host API fills the stats)
-        idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES)
+        idx.set_search_params(point[0], point[1], point[2], trees)
         res_host = idx.knn_search(10, q)
         st = idx.search_stats()
         evals_q = st.distance_evals / nq
@@ -193,7 +200,7 @@ def run_gpu(args):
         # (+ the FP32 rows re-ranked after BF16/FP8 screening)
         bytes_q = evals_q * row_bytes + exp_q * GRAPH["K"] * 4 + point[1] * 4 + 128 * 4 + st.reranked * 128 * 4
         for _ in range(args.warmup):
-            search_once(point)
+            search_once(point, trees)
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
@@ -203,7 +210,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
-            search_once(point)
+            search_once(point, trees)
         ev1.record(stream)
         torch.cuda.synchronize()
         replicas.barrier()
@@ -216,7 +223,7 @@ def run_gpu(args):
         for _ in range(args.steps):
             idx.knn_search(10, q)
         e2e_s = time.perf_counter() - t0
-        return {"precision": precision, "point": point, "ladder": ladder, "config_recall": res_cfg,
+        return {"precision": precision, "trees": trees, "point": point, "ladder": ladder, "config_recall": res_cfg,
                 "recall": recall(res_host, gt), "ms": ms, "per_step_ms": ms / args.steps,
                 "value": replicas.throughput(nq * args.steps, ms / 1e3, ws),
                 "e2e": replicas.throughput(nq * args.steps, replicas.max_over_ranks(e2e_s, dev), ws),
@@ -236,7 +243,9 @@ def run_gpu(args):
         if not measured:
             return None
         w = measured["workload"]
-        if (w["n"], w["queries"], tuple(w["point"])) != (args.n, nq, tuple(r["point"])):
+        pts = w.get("points", {})
+        if (w["n"], w["queries"], w["search_trees"]) != (args.n, nq, r["trees"]) or \
+                tuple(pts.get(r["precision"], ())) != tuple(r["point"]):
             return None
         return measured["per_step_bytes"].get(r["precision"])
 
@@ -292,6 +301,18 @@ def run_gpu(args):
         line["bf16_learned"] = learned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
+    if not args.no_wide:
+        t0 = time.perf_counter()
+        idx.build_trees(WIDE_TREES)
+        torch.cuda.synchronize()
+        wide_s = time.perf_counter() - t0
+        wide = {p: measure(p, WIDE_TREES, WIDE_LADDER) for p in ("fp32", "bf16", "fp8")}
+        line["trees48"] = {
+            "search_trees": WIDE_TREES, "trees_build_s": round(wide_s, 4),
+            "note": "the same search over 48 KD-trees instead of the configuration's 16",
+            **{p: {"value": round(r["value"], 1), "unit": "queries/s", "e2e": round(r["e2e"], 1),
+                   "operating_point": point_of(r), "ladder": r["ladder"], "roofline": roofline(r),
+                   "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"]} for p, r in wide.items()}}
     if not args.no_batching:
         idx.close()
         idx = None
@@ -399,19 +420,20 @@ def measure_batching(E, X, args):
 
 # settings that all fit the two-CTA-per-SM layout of the plain operating point, so that a batch mixing
 # them runs with that layout (a larger top rung would size every query's shared memory for itself)
-LEARNED_RUNGS = [(4, 600, 60), (6, 1200, 120), (6, 2000, 200), (8, 3000, 300), (8, 4000, 400),
-                 (8, 5000, 500), (8, 6000, 600)]
+LEARNED_RUNGS = [(4, 2400, 400), (4, 3000, 500), (4, 3000, 600), (4, 3500, 650), (4, 3500, 700), (4, 4000, 750),
+                 (4, 4500, 800), (4, 5000, 800)]
 
 
-def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args):
+def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
     """BF16 + learned: k-means entry clusters and an MLP trained on traces of held-out queries (their
     own exact neighbours and the plain search's recall per rung), then the learned search with the
     rung bias raised until recall@10 >= 0.95; device-timed like the plain arms."""
     import torch
     from efanna_gb300 import datasets
+    rungs = rungs or LEARNED_RUNGS
     idx.set_search_precision("bf16")
     t0 = time.perf_counter()
-    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=LEARNED_RUNGS,
+    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=rungs,
                   target=0.95, train_epochs=8, batch=1024, lr=1e-3)
     torch.cuda.synchronize()
     cluster_s = time.perf_counter() - t0
@@ -435,7 +457,7 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args):
         L.search_device(Q.data_ptr(), nq, 128, 10, out.data_ptr(), 0, stream.cuda_stream, cov)
         torch.cuda.synchronize()
         rc = recall(out.cpu().numpy(), gt)
-        pools = [LEARNED_RUNGS[i][1] for i in rung.cpu().numpy()]
+        pools = [rungs[i][1] for i in rung.cpu().numpy()]
         sweep.append({"coverage": cov, "recall@10": round(rc, 4), "mean_pool": round(float(np.mean(pools)), 1)})
         if rc >= TARGET:
             chosen = cov
@@ -454,13 +476,14 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args):
     ms = ev0.elapsed_time(ev1)
     res = {"value": round(ws * nq * args.steps / (ms / 1e3), 1), "unit": "queries/s",
            "ms_per_step": round(ms / args.steps, 4), "recall@10": sweep[-1]["recall@10"] if sweep else None,
-           "coverage": chosen, "sweep": sweep, "rungs": LEARNED_RUNGS,
-           "predicted_rung_histogram": np.bincount(r, minlength=len(LEARNED_RUNGS)).tolist(),
+           "coverage": chosen, "sweep": sweep, "rungs": rungs,
+           "predicted_rung_histogram": np.bincount(r, minlength=len(rungs)).tolist(),
            "train_queries": int(st.train_queries), "train_loss_first": round(st.train_loss_first, 4),
            "train_loss_last": round(st.train_loss_last, 4),
-           "plain_rung_recall_train": [round(st.rung_recall[i], 4) for i in range(len(LEARNED_RUNGS))],
+           "plain_rung_recall_train": [round(st.rung_recall[i], 4) for i in range(len(rungs))],
            "cluster_s": round(cluster_s, 3), "trace_and_train_s": round(train_s, 3),
-           "form": "MLP (128-256-256-(1024 clusters + 7 rungs), BF16 weights, FP32 accumulate) picks 8 entry "
+           "form": "MLP (128-256-256-(1024 clusters + %d rungs), BF16 weights, FP32 accumulate) picks 8 entry "
+                   % len(rungs) +
                    "clusters (8 seeds each) and a rung per query; BF16 screening, FP32 re-rank"}
     L.close()
     return res
@@ -577,6 +600,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--no-wide", action="store_true", help="skip the 48-tree measurement")
     ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()

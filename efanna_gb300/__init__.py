@@ -12,8 +12,10 @@ and a CUDA device and raises ``EfannaError`` otherwise.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -106,6 +108,23 @@ class IndexParams:
 
 
 _lib = None
+
+# library objects still open, by kind: closed at interpreter exit, dependents before their index,
+# while the CUDA runtime is still up (their destructors synchronise the index's stream)
+_live = {"learned": weakref.WeakSet(), "plan": weakref.WeakSet(), "hash": weakref.WeakSet(),
+         "index": weakref.WeakSet()}
+
+
+def _close_all():
+    for kind in ("learned", "plan", "hash", "index"):
+        for o in list(_live[kind]):
+            try:
+                o.close()
+            except Exception:
+                pass
+
+
+atexit.register(_close_all)
 
 
 def lib():
@@ -204,6 +223,7 @@ class Index:
         self._h = C.c_void_p()
         p = self.params.to_c()
         _check(lib().efg_index_create(_fp(data), self.n, self.dim, self.dim, C.byref(p), C.byref(self._h)))
+        _live["index"].add(self)
 
     @classmethod
     def from_device(cls, ptr: int, n: int, dim: int, row_stride: int, params: IndexParams | None = None):
@@ -213,6 +233,7 @@ class Index:
         self._h = C.c_void_p()
         p = self.params.to_c()
         _check(lib().efg_index_create_device(C.c_void_p(ptr), n, dim, row_stride, C.byref(p), C.byref(self._h)))
+        _live["index"].add(self)
         return self
 
     def close(self):
@@ -364,6 +385,7 @@ class SearchPlan:
                                             None if cq is None else _fp(cq), 0 if cq is None else cq.shape[0],
                                             C.byref(h)))
         self._h = h
+        _live["plan"].add(self)
 
     @property
     def threads(self) -> int:
@@ -412,6 +434,7 @@ class Learned:
         h = C.c_void_p()
         _check(lib().efg_learned_create(index._h, C.byref(p), C.byref(h)))
         self._h = h
+        _live["learned"].add(self)
 
     @property
     def rungs(self):
@@ -498,6 +521,7 @@ class HashTables:
         _check(lib().efg_hash_create(index._h, C.c_void_p(c.ctypes.data), c.shape[0], code_bits, radius,
                                      C.byref(h)))
         self._h = h
+        _live["hash"].add(self)
 
     @property
     def ball_size(self) -> int:

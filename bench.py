@@ -301,6 +301,8 @@ def run_gpu(args):
         line["bf16_learned"] = learned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
+    if not args.no_hashing:
+        line["hashing"] = measure_hashing(E, idx, x, q, Q, gt, nq, stream, ws, args)
     if not args.no_wide:
         t0 = time.perf_counter()
         idx.build_trees(WIDE_TREES)
@@ -489,6 +491,83 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
     return res
 
 
+# the hashing-seeded search: 8 tables of 20-bit sign-of-projection codes, Hamming radius 2
+HASH_TABLES, HASH_BITS, HASH_RADIUS = 8, 20, 2
+HASH_LADDER = [(4, 4000, 750), (4, 5000, 800), (4, 6000, 800), (6, 8000, 1000)]
+
+
+def measure_hashing(E, idx, x, q, Q, gt, nq, stream, ws, args):
+    """The hashing initialiser's pool/extend search (search method 1 of the hashing index) on the
+    same graph: codes from seeded hyperplanes (the reference reads externally made code files),
+    hash tables built once, then the first ladder setting reaching recall@10 >= 0.95, device-timed
+    and end to end through the host API; the oracle's restatement on the host cores beside it."""
+    import torch
+    from efanna_gb300 import datasets
+    idx.set_search_precision("fp32")
+    mean = x.mean(0)
+    t0 = time.perf_counter()
+    bc = datasets.sign_codes(x, HASH_TABLES, HASH_BITS, seed=1, center=mean)
+    qc = datasets.sign_codes(q, HASH_TABLES, HASH_BITS, seed=1, center=mean)
+    codes_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ht = E.HashTables(idx, bc, HASH_BITS, HASH_RADIUS)
+    tables_s = time.perf_counter() - t0
+    QC = torch.from_numpy(qc.view(np.int64)).cuda()
+    out = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+
+    def run(pt):
+        idx.set_search_params(pt[0], pt[1], pt[2], 1, -1, 1)
+        ht.search_device(Q.data_ptr(), nq, 128, QC.data_ptr(), nq, 10, out.data_ptr(), stream.cuda_stream)
+
+    ladder, point = [], None
+    for pt in HASH_LADDER:
+        run(pt)
+        torch.cuda.synchronize()
+        rc = recall(out.cpu().numpy(), gt)
+        ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4)})
+        if rc >= TARGET:
+            point = pt
+            break
+    point = point or HASH_LADDER[-1]
+    for _ in range(args.warmup):
+        run(point)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run(point)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ht.search(10, q, qc)
+    e2e_s = time.perf_counter() - t0
+    res = {"value": round(ws * nq * args.steps / (ms / 1e3), 1), "unit": "queries/s",
+           "e2e": round(ws * nq * args.steps / e2e_s, 1), "ms_per_step": round(ms / args.steps, 4),
+           "operating_point": ladder[-1], "ladder": ladder,
+           "codes": {"tables": HASH_TABLES, "bits": HASH_BITS, "radius": HASH_RADIUS, "ball": ht.ball_size,
+                     "make_codes_s": round(codes_s, 3), "tables_build_s": round(tables_s, 3)},
+           "gpu_launches_per_step": 2 + 1,
+           "form": "hash seed rows (Hamming-ball probe kernel) then nnexp_kernel without trees"}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        gp, gi = idx.graph_csr()
+        m = min(nq, args.cpu_queries)
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ids, _ = O.search_hashed(x, gp, gi, q[:m], bc, qc[:, :m], HASH_BITS, HASH_RADIUS, k=10, epochs=point[0],
+                                 init_num=point[1], extend_to=point[2], mode=O.CANON, threads=cores)
+        cpu_s = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": round(m / cpu_s, 1), "unit": "queries/s", "cores": cores, "kind": "port",
+                               "sample": "%d of %d queries, same codes/graph/operating point" % (m, nq),
+                               "recall@10": round(recall(ids, gt[:m]), 4)}
+    ht.close()
+    return res
+
+
 def cpu_baseline(x, q, gt, point, idx, args):
     """The oracle's search (reference nnexp semantics, OpenMP over queries) on the GPU-built trees
     and graph, over a bounded sample of the queries."""
@@ -601,6 +680,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-wide", action="store_true", help="skip the 48-tree measurement")
+    ap.add_argument("--no-hashing", action="store_true", help="skip the hashing-seeded search")
     ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()

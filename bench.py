@@ -301,6 +301,8 @@ def run_gpu(args):
         line["bf16_learned"] = learned
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, q, gt, f32["point"], idx, args)
+    if not args.no_kgraph:
+        line["kgraph"] = measure_kgraph(E, idx, Q, gt, nq, stream, ws, args)
     if not args.no_hashing:
         line["hashing"] = measure_hashing(E, idx, x, q, Q, gt, nq, stream, ws, args)
     if not args.no_wide:
@@ -491,6 +493,48 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
     return res
 
 
+# kgraph search (search method 1) settings in ascending cost
+KGRAPH_LADDER = [(4, 1200, 200), (4, 2400, 300), (6, 3000, 400), (6, 4000, 500), (8, 6000, 600)]
+
+
+def measure_kgraph(E, idx, Q, gt, nq, stream, ws, args):
+    """Search method 1 (getNeighbors_kgraph) on the same index and trees: the first ladder setting
+    reaching recall@10 >= 0.95, device-timed."""
+    import torch
+    idx.set_search_precision("fp32")
+    out = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+
+    def run(pt):  # the reference keeps an enlarged pool size; start every call from the setting's own
+        idx.set_search_params(pt[0], pt[1], pt[2], SEARCH_TREES, -1, 1)
+        idx.knn_search_device(10, Q.data_ptr(), nq, 128, out.data_ptr(), stream.cuda_stream)
+
+    ladder, point = [], None
+    for pt in KGRAPH_LADDER:
+        run(pt)
+        torch.cuda.synchronize()
+        rc = recall(out.cpu().numpy(), gt)
+        ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4)})
+        if rc >= TARGET:
+            point = pt
+            break
+    point = point or KGRAPH_LADDER[-1]
+    for _ in range(args.warmup):
+        run(point)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run(point)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    idx.set_search_params(point[0], point[1], point[2], SEARCH_TREES, -1, 0)
+    return {"value": round(ws * nq * args.steps / (ms / 1e3), 1), "unit": "queries/s",
+            "ms_per_step": round(ms / args.steps, 4), "operating_point": ladder[-1], "ladder": ladder,
+            "search_trees": SEARCH_TREES,
+            "form": "nnexp_kernel pool stage (keys in pool order), row sort when sorted, kgraph_kernel"}
+
+
 # the hashing-seeded search: 8 tables of 20-bit sign-of-projection codes, Hamming radius 2
 HASH_TABLES, HASH_BITS, HASH_RADIUS = 8, 20, 2
 HASH_LADDER = [(4, 4000, 750), (4, 5000, 800), (4, 6000, 800), (6, 8000, 1000)]
@@ -669,7 +713,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
@@ -681,6 +725,7 @@ def main():
     ap.add_argument("--no-batching", action="store_true")
     ap.add_argument("--no-wide", action="store_true", help="skip the 48-tree measurement")
     ap.add_argument("--no-hashing", action="store_true", help="skip the hashing-seeded search")
+    ap.add_argument("--no-kgraph", action="store_true", help="skip the kgraph search (method 1)")
     ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()

@@ -468,6 +468,10 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
             break
     if chosen is None:
         chosen = 0.995
+    r_argmax = r
+    L.predict_device(Q.data_ptr(), nq, 128, clusters.data_ptr(), rung.data_ptr(), stream.cuda_stream, chosen)
+    torch.cuda.synchronize()
+    r = rung.cpu().numpy()  # the rungs the timed search uses
     for _ in range(args.warmup):
         L.search_device(Q.data_ptr(), nq, 128, 10, out.data_ptr(), 0, stream.cuda_stream, chosen)
     torch.cuda.synchronize()
@@ -481,7 +485,9 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
     res = {"value": round(ws * nq * args.steps / (ms / 1e3), 1), "unit": "queries/s",
            "ms_per_step": round(ms / args.steps, 4), "recall@10": sweep[-1]["recall@10"] if sweep else None,
            "coverage": chosen, "sweep": sweep, "rungs": rungs,
-           "predicted_rung_histogram": np.bincount(r, minlength=len(rungs)).tolist(),
+           "rung_histogram_at_coverage": np.bincount(r, minlength=len(rungs)).tolist(),
+           "most_likely_rung_histogram": np.bincount(r_argmax, minlength=len(rungs)).tolist(),
+           "mean_pool": round(float(np.mean([rungs[i][1] for i in r])), 1),
            "train_queries": int(st.train_queries), "train_loss_first": round(st.train_loss_first, 4),
            "train_loss_last": round(st.train_loss_last, 4),
            "plain_rung_recall_train": [round(st.rung_recall[i], 4) for i in range(len(rungs))],

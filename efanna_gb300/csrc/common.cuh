@@ -118,4 +118,26 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// Sums v[0..8) over the warp's 32 lanes; lane l returns the total of v[(l >> 2) & 7].  At each
+// exchange a lane keeps the half of its values that its partner sends it the other half of.
+__device__ __forceinline__ float reduce8_rows(const float* v, uint32_t lane) {
+  const bool b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1, b2 = (lane >> 2) & 1;
+  float h[4], q[2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    float keep = b4 ? v[j + 4] : v[j], send = b4 ? v[j] : v[j + 4];
+    h[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    float keep = b3 ? h[j + 2] : h[j], send = b3 ? h[j] : h[j + 2];
+    q[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  float keep = b2 ? q[1] : q[0], send = b2 ? q[0] : q[1];
+  float x = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  x += __shfl_xor_sync(0xffffffffu, x, 2);
+  x += __shfl_xor_sync(0xffffffffu, x, 1);
+  return x;
+}
+
 }  // namespace efg

@@ -386,9 +386,12 @@ __global__ void join_kernel(const float* __restrict__ base, uint32_t ld4, uint64
               acc[u] += d3 * d3;
             }
           }
+          // the eight row sums reduced together (lanes 4r .. 4r+3 end with row r's), then row
+          // u's sum moves to lane u0 + u
+          float tot = reduce8_rows(acc, lane);
+          float d = __shfl_sync(0xffffffffu, tot, ((lane - u0) & 7) * 4);
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
-            float d = warp_sum(acc[u]);
             if (lane == u0 + u) {
               mine = d;
               my_y = yy[u];

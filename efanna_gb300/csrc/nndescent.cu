@@ -331,8 +331,10 @@ __global__ void bound_kernel(uint64_t n, uint32_t P, const float* __restrict__ p
   bound[t] = r > w ? r : w;
 }
 
-// One warp per node i.  Pass 0: distances of all its pairs (stored) and record counts per
-// target.  Pass 1: records written from the stored distances.
+// One warp per node i, nodes taken from a shared counter as warps come free (nodes' pair counts
+// differ by an order of magnitude, so fixed assignment leaves most warps of a block idle behind
+// its longest node).  Pass 0: distances of all its pairs (stored) and record counts per target.
+// Pass 1: records written from the stored distances.
 template <int PASS>
 __global__ void join_kernel(const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P,
                             uint32_t check_k, const uint32_t* __restrict__ new_ids,
@@ -341,12 +343,16 @@ __global__ void join_kernel(const float* __restrict__ base, uint32_t ld4, uint64
                             const float* __restrict__ bound, float* __restrict__ pairdist,
                             uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off,
                             uint32_t* __restrict__ cursor, uint64_t* __restrict__ rec_key,
-                            uint32_t* __restrict__ rec_aux, uint8_t* __restrict__ found) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint32_t lane = threadIdx.x & 31;
+                            uint32_t* __restrict__ rec_aux, uint8_t* __restrict__ found,
+                            uint32_t* __restrict__ next_node) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+  uint32_t ii = 0;
+  if (lane == 0) ii = atomicAdd(next_node, 1u);
+  const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
   if (i >= n) return;
   uint32_t nn = new_cnt[i], no = old_cnt[i];
-  if (nn == 0) return;
+  if (nn == 0) continue;
   const uint32_t* nw = new_ids + i * cap;
   const uint32_t* od = old_ids + i * cap;
   uint64_t po = pair_off[i];
@@ -443,6 +449,7 @@ __global__ void join_kernel(const float* __restrict__ base, uint32_t ld4, uint64
     }
   }
   if (PASS == 0 && __any_sync(0xffffffffu, found_drop) && lane == 0) found[i] = 1;
+  }
 }
 
 // Pool of one node held by a warp: entry e on lane e % 32, slot e / 32.
@@ -848,9 +855,19 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.found.p, 0, n, s));
-  join_kernel<0><<<blocks_for(n * 32, 256), 256, 0, s>>>(
+  DevBuf<uint32_t> jctr;  // the two passes' node counters
+  EFG_TRY(jctr.reserve(2));
+  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 8, s));
+  int sms = 152, per0 = 1, per1 = 1, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, join_kernel<0>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, join_kernel<1>, 256, 0);
+  const unsigned jgrid0 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per0, 1));
+  const unsigned jgrid1 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per1, 1));
+  join_kernel<0><<<jgrid0, 256, 0, s>>>(
       idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p,
-      bound.p, S.pairdist.p, S.cnt.p, nullptr, nullptr, nullptr, nullptr, S.found.p);
+      bound.p, S.pairdist.p, S.cnt.p, nullptr, nullptr, nullptr, nullptr, S.found.p, jctr.p);
   EFG_CUDA(cudaGetLastError());
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, tmp64.p, n);
   EFG_TRY(device_scan<uint64_t>(tmp64.p, n, S.rec_off64.p, S.scan64.p, s));
@@ -859,9 +876,9 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaStreamSynchronize(s));
   EFG_TRY(S.rec_key.reserve(nrec + 1));
   EFG_TRY(S.rec_aux.reserve(nrec + 1));
-  join_kernel<1><<<blocks_for(n * 32, 256), 256, 0, s>>>(
+  join_kernel<1><<<jgrid1, 256, 0, s>>>(
       idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p,
-      bound.p, S.pairdist.p, S.cnt.p, S.rec_off64.p, S.cursor.p, S.rec_key.p, S.rec_aux.p, S.found.p);
+      bound.p, S.pairdist.p, S.cnt.p, S.rec_off64.p, S.cursor.p, S.rec_key.p, S.rec_aux.p, S.found.p, jctr.p + 1);
   EFG_CUDA(cudaGetLastError());
   if (S.P <= 32)
     merge_kernel<1><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,

@@ -336,7 +336,7 @@ __global__ void bound_kernel(uint64_t n, uint32_t P, const float* __restrict__ p
 // its longest node).  Pass 0: distances of all its pairs (stored) and record counts per target.
 // Pass 1: records written from the stored distances.
 template <int PASS>
-__global__ void join_kernel(const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P,
+__global__ void __launch_bounds__(256, 4) join_kernel(const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P,
                             uint32_t check_k, const uint32_t* __restrict__ new_ids,
                             const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids,
                             const uint32_t* __restrict__ old_cnt, const uint64_t* __restrict__ pair_off,

@@ -138,12 +138,21 @@ __global__ void merge_route_kernel(const float* __restrict__ base, uint32_t ld4,
   unsigned long long local = 0;
   const float* fb = base;
   for (; w < ntasks; w += nw) {
-    // node owning task w: last v with task_off[v] <= w
+    // node owning task w: last v with task_off[v] <= w, searched by the whole warp (32 probes a
+    // round, so about five dependent rounds instead of a load per halving)
     uint64_t lo = 0, hi = nnodes;
-    while (hi - lo > 1) {
-      uint64_t mid = (lo + hi) >> 1;
-      if (task_off[mid] <= w) lo = mid;
-      else hi = mid;
+    while (hi - lo > 32) {
+      uint64_t step = (hi - lo + 31) / 32;
+      uint64_t probe = lo + (uint64_t)lane * step;
+      bool le = probe < hi && task_off[probe] <= w;  // true for a prefix of the lanes (lane 0 always)
+      uint32_t k = 31 - __clz(__ballot_sync(0xffffffffu, le));
+      lo += (uint64_t)k * step;
+      hi = min(hi, lo + step);
+    }
+    {
+      uint64_t probe = lo + lane;
+      bool le = probe < hi && task_off[probe] <= w;
+      lo += 31 - __clz(__ballot_sync(0xffffffffu, le));
     }
     uint64_t v = lo;
     int32_t L = tv.left[v], R = tv.right[v];
@@ -161,11 +170,38 @@ __global__ void merge_route_kernel(const float* __restrict__ base, uint32_t ld4,
       nd = tv.nodes[cur];
     }
     uint32_t ls = (uint32_t)(-(nd.left + 1)), le = (uint32_t)nd.right;
-    for (uint32_t i = ls; i < le; ++i) {
-      uint32_t q = ll[i];
-      float d = warp_sum(lane_l2_rows(base, ld4, q, p));
-      ++local;
-      if (lane == 0) {
+    const float4* rp = reinterpret_cast<const float4*>(base) + (uint64_t)p * ld4;
+    for (uint32_t i0 = ls; i0 < le; i0 += 8) {  // eight leaf points at a time, their loads in flight together
+      const uint32_t cnt8 = min(8u, le - i0);
+      uint32_t qq[8];
+      float acc[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        qq[u] = ll[i0 + min((uint32_t)u, cnt8 - 1)];
+        acc[u] = 0.f;
+      }
+      for (uint32_t c = lane; c < ld4; c += 32) {
+        float4 y = __ldg(rp + c);
+        float4 x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = __ldg(reinterpret_cast<const float4*>(base) + (uint64_t)qq[u] * ld4 + c);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float d0 = x[u].x - y.x, d1 = x[u].y - y.y, d2 = x[u].z - y.z, d3 = x[u].w - y.w;
+          acc[u] += d0 * d0;
+          acc[u] += d1 * d1;
+          acc[u] += d2 * d2;
+          acc[u] += d3 * d3;
+        }
+      }
+      const float d = reduce8_rows(acc, lane);  // lanes 4r .. 4r+3: leaf point r's distance
+      const uint32_t r = lane >> 2;
+      uint32_t q = qq[0];
+#pragma unroll
+      for (int u = 1; u < 8; ++u)
+        if (r == (uint32_t)u) q = qq[u];
+      local += cnt8;
+      if ((lane & 3) == 0 && r < cnt8) {
         if (PASS == 0) {
           atomicAdd(&cnt[q], 1u);
           atomicAdd(&cnt[p], 1u);

@@ -127,7 +127,7 @@ __global__ void min_leaf_level_kernel(TreeView tv, uint64_t nnodes, uint32_t tre
 // kdtreeub_index.hpp:1012-1021) and compare with each leaf point.  pass 0 counts records per
 // target, pass 1 writes them: key = (dist bits << 32) | candidate.
 template <int PASS>
-__global__ void merge_route_kernel(const float* __restrict__ base, uint32_t ld4, TreeView tv,
+__global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __restrict__ base, uint32_t ld4, TreeView tv,
                                    const uint64_t* __restrict__ task_off, uint64_t nnodes, uint64_t ntasks,
                                    uint32_t* __restrict__ cnt, const uint64_t* __restrict__ off,
                                    uint32_t* __restrict__ cursor, uint64_t* __restrict__ keys,

@@ -32,6 +32,15 @@ struct DevBuf {
   }
 };
 
+// A function-local device buffer: freed when it goes out of scope (also on early error returns).
+template <typename T>
+struct LocalBuf : DevBuf<T> {
+  LocalBuf() = default;
+  LocalBuf(const LocalBuf&) = delete;
+  LocalBuf& operator=(const LocalBuf&) = delete;
+  ~LocalBuf() { this->release(); }
+};
+
 // Host-side tree node (load/save and the merge-level check).
 struct HNode {
   int32_t div_dim;

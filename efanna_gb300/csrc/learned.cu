@@ -451,12 +451,6 @@ struct efg_learned {
 
 namespace {
 
-// A device buffer freed when it leaves scope (locals of the build steps).
-template <typename T>
-struct ScopedBuf : DevBuf<T> {
-  ~ScopedBuf() { this->release(); }
-};
-
 uint64_t nparams(uint32_t H, uint32_t din, uint32_t O) {
   return (uint64_t)H * din + H + (uint64_t)H * H + H + (uint64_t)O * H + O;
 }
@@ -601,10 +595,10 @@ int efg_learned_create(efg_index* idx, const efg_learned_params* params, efg_lea
   // 1. sample (a Feistel permutation of the base, seeded) and k-means
   std::vector<uint32_t> rows(S);
   for (uint64_t i = 0; i < S; ++i) rows[i] = feistel_perm((uint32_t)i, (uint32_t)idx->n, p.seed ^ 0x6b6d65616e73ULL);
-  ScopedBuf<uint32_t> drows;
-  ScopedBuf<float> sample;
-  ScopedBuf<int32_t> sassign;
-  ScopedBuf<float> sdist;
+  LocalBuf<uint32_t> drows;
+  LocalBuf<float> sample;
+  LocalBuf<int32_t> sassign;
+  LocalBuf<float> sdist;
   if ((rc = drows.reserve(S)) || (rc = sample.reserve(S * ld)) || (rc = sassign.reserve(S)) ||
       (rc = sdist.reserve(S)) || (rc = L->cent.reserve((uint64_t)L->Cn * ld)) || (rc = L->mean.reserve(ld)) ||
       (rc = L->istd.reserve(ld)))
@@ -684,8 +678,8 @@ int efg_learned_train(efg_learned* L, const float* d_q, uint64_t n, uint64_t row
   EFG_CUDA(cudaMemsetAsync(L->trainq.p, 0, n * ld * 4, s));
   EFG_CUDA(cudaMemcpy2DAsync(L->trainq.p, ld * 4, d_q, row_stride * 4, dim * 4, n, cudaMemcpyDeviceToDevice, s));
   // traces: exact neighbours, their clusters, recall per rung, labels
-  ScopedBuf<int32_t> gt, res;
-  ScopedBuf<float> gtd, rec;
+  LocalBuf<int32_t> gt, res;
+  LocalBuf<float> gtd, rec;
   EFG_TRY(gt.reserve(n * GT_K));
   EFG_TRY(gtd.reserve(n * GT_K));
   EFG_TRY(rec.reserve(n * R));
@@ -834,8 +828,8 @@ int efg_learned_grad(efg_learned* L, const float* d_x, uint32_t B, uint64_t row_
   cudaStream_t s = L->idx->stream;
   EFG_TRY(reserve_batch(L, B));
   // targets for rows 0..B-1 taken from the caller's arrays
-  ScopedBuf<uint32_t> tc;
-  ScopedBuf<uint8_t> tl;
+  LocalBuf<uint32_t> tc;
+  LocalBuf<uint8_t> tl;
   EFG_TRY(tc.reserve((uint64_t)B * GT_K));
   EFG_TRY(tl.reserve(B));
   EFG_CUDA(cudaMemcpyAsync(tc.p, d_tclusters, (uint64_t)B * GT_K * 4, cudaMemcpyDeviceToDevice, s));

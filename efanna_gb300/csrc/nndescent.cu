@@ -125,13 +125,16 @@ __global__ void min_leaf_level_kernel(TreeView tv, uint64_t nnodes, uint32_t tre
 
 // One warp per routed point: descend the larger child to a leaf (SearchToLeaf,
 // kdtreeub_index.hpp:1012-1021) and compare with each leaf point.  pass 0 counts records per
-// target, pass 1 writes them: key = (dist bits << 32) | candidate.
+// target, pass 1 writes them: key = (dist bits << 32) | candidate.  With task_d set, pass 0 also
+// keeps each task's point, leaf and distances (maxl per task), and merge_emit_kernel writes the
+// records from them instead of a second routing pass.
 template <int PASS>
 __global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __restrict__ base, uint32_t ld4, TreeView tv,
                                    const uint64_t* __restrict__ task_off, uint64_t nnodes, uint64_t ntasks,
                                    uint32_t* __restrict__ cnt, const uint64_t* __restrict__ off,
                                    uint32_t* __restrict__ cursor, uint64_t* __restrict__ keys,
-                                   unsigned long long* __restrict__ ndist) {
+                                   unsigned long long* __restrict__ ndist, uint32_t* __restrict__ task_p,
+                                   int32_t* __restrict__ task_leaf, float* __restrict__ task_d, uint32_t maxl) {
   uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   uint32_t lane = threadIdx.x & 31;
@@ -170,6 +173,10 @@ __global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __rest
       nd = tv.nodes[cur];
     }
     uint32_t ls = (uint32_t)(-(nd.left + 1)), le = (uint32_t)nd.right;
+    if (PASS == 0 && task_d && lane == 0) {
+      task_p[w] = p;
+      task_leaf[w] = cur;
+    }
     const float4* rp = reinterpret_cast<const float4*>(base) + (uint64_t)p * ld4;
     for (uint32_t i0 = ls; i0 < le; i0 += 8) {  // eight leaf points at a time, their loads in flight together
       const uint32_t cnt8 = min(8u, le - i0);
@@ -203,6 +210,7 @@ __global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __rest
       local += cnt8;
       if ((lane & 3) == 0 && r < cnt8) {
         if (PASS == 0) {
+          if (task_d) task_d[w * maxl + (i0 - ls) + r] = d;
           atomicAdd(&cnt[q], 1u);
           atomicAdd(&cnt[p], 1u);
         } else {
@@ -215,6 +223,36 @@ __global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __rest
     }
   }
   if (PASS == 0 && lane == 0 && local) atomicAdd(ndist, local);
+}
+
+// Records of the leaf merge from what pass 0 kept: one thread per task.
+__global__ void merge_emit_kernel(TreeView tv, uint64_t ntasks, const uint32_t* __restrict__ task_p,
+                                  const int32_t* __restrict__ task_leaf, const float* __restrict__ task_d,
+                                  uint32_t maxl, const uint64_t* __restrict__ off, uint32_t* __restrict__ cursor,
+                                  uint64_t* __restrict__ keys) {
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < ntasks;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = task_p[w];
+    const int32_t leaf = task_leaf[w];
+    const DNode nd = tv.nodes[leaf];
+    const uint32_t* ll = tv.leaves + (uint64_t)tv.tree[leaf] * tv.n;
+    const uint32_t ls = (uint32_t)(-(nd.left + 1)), le = (uint32_t)nd.right;
+    for (uint32_t i = ls; i < le; ++i) {
+      const uint32_t q = ll[i];
+      const float d = task_d[w * maxl + (i - ls)];
+      uint32_t a = atomicAdd(&cursor[q], 1u);
+      keys[off[q] + a] = pack_key(d, p);
+      uint32_t b = atomicAdd(&cursor[p], 1u);
+      keys[off[p] + b] = pack_key(d, q);
+    }
+  }
+}
+
+// Largest leaf of the forest (points per leaf).
+__global__ void max_leaf_kernel(TreeView tv, uint64_t nnodes, uint32_t* __restrict__ out) {
+  uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nnodes) return;
+  if (tv.left[v] < 0) atomicMax(out, (uint32_t)(tv.end[v] - tv.start[v]));
 }
 
 // Position of x in the ascending warp-distributed list t (number of elements < x), or -1 if an
@@ -781,7 +819,7 @@ __global__ void widen_kernel(const uint32_t* __restrict__ in, uint64_t* __restri
 static int merge_level_check(efg_index* idx, int32_t* min_level) {
   Forest& F = idx->forest;
   TreeView tv{F.nodes.p, F.n_left.p, F.n_right.p, F.n_level.p, F.n_tree.p, F.n_start.p, F.n_end.p, F.leaves.p, F.n};
-  DevBuf<int32_t> d;
+  LocalBuf<int32_t> d;
   EFG_TRY(d.reserve(1));
   int32_t big = 0x7fffffff;
   EFG_CUDA(cudaMemcpyAsync(d.p, &big, 4, cudaMemcpyHostToDevice, idx->stream));
@@ -825,18 +863,39 @@ static int nnd_init_device(efg_index* idx, NNDev& S) {
   // per-target record counts -> offsets
   EFG_TRY(S.cnt.reserve(n));
   EFG_TRY(S.cursor.reserve(n));
-  DevBuf<uint64_t> cnt64, off64;
+  LocalBuf<uint64_t> cnt64, off64;
   EFG_TRY(cnt64.reserve(n));
   EFG_TRY(off64.reserve(n + 1));
-  DevBuf<unsigned long long> nd;
+  LocalBuf<unsigned long long> nd;
   EFG_TRY(nd.reserve(1));
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(nd.p, 0, 8, s));
   unsigned rgrid = (unsigned)std::min<uint64_t>(blocks_for(ntasks * 32, 256), 152ull * 64);
+  // what pass 0 keeps for the record pass: the point, the leaf and maxl distances per task (when
+  // that stays within 4 GiB; otherwise pass 1 routes again)
+  uint32_t maxl = 0;
+  {
+    LocalBuf<uint32_t> ml;
+    EFG_TRY(ml.reserve(1));
+    EFG_CUDA(cudaMemsetAsync(ml.p, 0, 4, s));
+    max_leaf_kernel<<<blocks_for(F.nnodes, 256), 256, 0, s>>>(tv, F.nnodes, ml.p);
+    EFG_CUDA(cudaMemcpyAsync(&maxl, ml.p, 4, cudaMemcpyDeviceToHost, s));
+    EFG_CUDA(cudaStreamSynchronize(s));
+  }
+  const bool keep = ntasks && maxl && ntasks * (uint64_t)(maxl + 2) * 4 <= (4ull << 30);
+  LocalBuf<uint32_t> task_p;
+  LocalBuf<int32_t> task_leaf;
+  LocalBuf<float> task_d;
+  if (keep) {
+    EFG_TRY(task_p.reserve(ntasks));
+    EFG_TRY(task_leaf.reserve(ntasks));
+    EFG_TRY(task_d.reserve(ntasks * maxl));
+  }
   if (ntasks) {
     merge_route_kernel<0><<<rgrid, 256, 0, s>>>(idx->d_base, ld4, tv, S.rec_off64.p, F.nnodes, ntasks, S.cnt.p,
-                                                 nullptr, nullptr, nullptr, nd.p);
+                                                 nullptr, nullptr, nullptr, nd.p, task_p.p, task_leaf.p, task_d.p,
+                                                 maxl);
     EFG_CUDA(cudaGetLastError());
   }
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, cnt64.p, n);
@@ -849,9 +908,14 @@ static int nnd_init_device(efg_index* idx, NNDev& S) {
   EFG_CUDA(cudaStreamSynchronize(s));
   idx->bstats.merge_distances = ndist;
   EFG_TRY(S.rec_key.reserve(nrec + 1));
-  if (ntasks) {
+  if (keep) {
+    merge_emit_kernel<<<(unsigned)std::min<uint64_t>(blocks_for(ntasks, 256), 152ull * 64), 256, 0, s>>>(
+        tv, ntasks, task_p.p, task_leaf.p, task_d.p, maxl, off64.p, S.cursor.p, S.rec_key.p);
+    EFG_CUDA(cudaGetLastError());
+  } else if (ntasks) {
     merge_route_kernel<1><<<rgrid, 256, 0, s>>>(idx->d_base, ld4, tv, S.rec_off64.p, F.nnodes, ntasks, nullptr,
-                                                off64.p, S.cursor.p, S.rec_key.p, nullptr);
+                                                off64.p, S.cursor.p, S.rec_key.p, nullptr, nullptr, nullptr, nullptr,
+                                                0);
     EFG_CUDA(cudaGetLastError());
   }
   init_select_kernel<<<blocks_for(n * 32, 256), 256, 0, s>>>(
@@ -874,7 +938,7 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_TRY(S.pair_off.reserve(n + 1));
   EFG_TRY(S.rec_off64.reserve(n + 1));
   EFG_TRY(S.scan64.reserve(scan_tmp_elems<uint64_t>(2 * n) + 1));
-  DevBuf<uint64_t> tmp64;
+  LocalBuf<uint64_t> tmp64;
   EFG_TRY(tmp64.reserve(2 * n + 1));
   pair_count_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, S.new_cnt.p, S.old_cnt.p, tmp64.p);
   EFG_CUDA(cudaGetLastError());
@@ -885,13 +949,13 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_TRY(S.pairdist.reserve(npairs + 1));
   EFG_TRY(S.cnt.reserve(2 * n));
   EFG_TRY(S.cursor.reserve(2 * n));
-  DevBuf<float> bound;
+  LocalBuf<float> bound;
   EFG_TRY(bound.reserve(n));
   bound_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, S.P, S.pd.p, S.Lc.p, S.radius.p, bound.p);
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.found.p, 0, n, s));
-  DevBuf<uint32_t> jctr;  // the two passes' node counters
+  LocalBuf<uint32_t> jctr;  // the two passes' node counters
   EFG_TRY(jctr.reserve(2));
   EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 8, s));
   int sms = 152, per0 = 1, per1 = 1, dev = 0;

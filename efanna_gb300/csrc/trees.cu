@@ -323,9 +323,9 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
   const uint64_t cap_nodes = 2 * total + ntrees;  // each split adds two nodes; at most n-1 splits per tree
 
   EFG_TRY(F.leaves.reserve(total));
-  DevBuf<uint32_t> ids_b;
-  DevBuf<int32_t> owner;
-  DevBuf<uint64_t> flags, pref, scan_tmp;
+  LocalBuf<uint32_t> ids_b;
+  LocalBuf<int32_t> owner;
+  LocalBuf<uint64_t> flags, pref, scan_tmp;
   EFG_TRY(ids_b.reserve(total));
   EFG_TRY(owner.reserve(total));
   EFG_TRY(flags.reserve(total));
@@ -337,8 +337,8 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
   EFG_TRY(F.n_level.reserve(cap_nodes));
   EFG_TRY(F.n_left.reserve(cap_nodes));
   EFG_TRY(F.n_right.reserve(cap_nodes));
-  DevBuf<int32_t> n_dim, n_split;
-  DevBuf<float> n_val;
+  LocalBuf<int32_t> n_dim, n_split;
+  LocalBuf<float> n_val;
   EFG_TRY(n_dim.reserve(cap_nodes));
   EFG_TRY(n_split.reserve(cap_nodes));
   EFG_TRY(n_val.reserve(cap_nodes));
@@ -346,8 +346,8 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
 
   // active lists and per-level scratch (active count <= total)
   uint64_t cap_act = std::max<uint64_t>(total, 2048);
-  DevBuf<int32_t> act, next_cand;
-  DevBuf<uint32_t> split_flag, child_off, mids, next_flag, next_pos, tmp32;
+  LocalBuf<int32_t> act, next_cand;
+  LocalBuf<uint32_t> split_flag, child_off, mids, next_flag, next_pos, tmp32;
   EFG_TRY(act.reserve(cap_act));
   EFG_TRY(next_cand.reserve(2 * cap_act));
   EFG_TRY(split_flag.reserve(cap_act));

@@ -440,23 +440,27 @@ __global__ void __launch_bounds__(256, 4) join_kernel(const float* __restrict__ 
       uint32_t my_y = 0;
       bool my_new = false;
       if (PASS == 0) {
+        // lane l's candidate (position cb + l; the last one repeated past cm), loaded once per chunk
+        // and handed to the passes by shuffles
+        const uint32_t cl = cb + min(lane, cm - 1);
+        const uint32_t cand = cl < nn - 1 - p ? nw[p + 1 + cl] : od[cl - (nn - 1 - p)];
+        my_y = cand;
+        const float4* rx = reinterpret_cast<const float4*>(base) + (uint64_t)x * ld4;
         // 8 rows in flight per lane
         for (uint32_t u0 = 0; u0 < cm; u0 += 8) {
           float acc[8];
-          uint32_t yy[8];
+          const float4* ry[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
-            uint32_t c = cb + u0 + u;
-            uint32_t cc = min(c, cb + cm - 1);
-            yy[u] = cc < nn - 1 - p ? nw[p + 1 + cc] : od[cc - (nn - 1 - p)];
+            uint32_t yu = __shfl_sync(0xffffffffu, cand, min(u0 + u, cm - 1));
+            ry[u] = reinterpret_cast<const float4*>(base) + (uint64_t)yu * ld4;
             acc[u] = 0.f;
           }
-          const float4* rx = reinterpret_cast<const float4*>(base) + (uint64_t)x * ld4;
           for (uint32_t c4 = lane; c4 < ld4; c4 += 32) {
             float4 xv = __ldg(rx + c4);
             float4 yv[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) yv[u] = __ldg(reinterpret_cast<const float4*>(base) + (uint64_t)yy[u] * ld4 + c4);
+            for (int u = 0; u < 8; ++u) yv[u] = __ldg(ry[u] + c4);
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
               float d0 = xv.x - yv[u].x, d1 = xv.y - yv[u].y, d2 = xv.z - yv[u].z, d3 = xv.w - yv[u].w;
@@ -470,13 +474,7 @@ __global__ void __launch_bounds__(256, 4) join_kernel(const float* __restrict__ 
           // u's sum moves to lane u0 + u
           float tot = reduce8_rows(acc, lane);
           float d = __shfl_sync(0xffffffffu, tot, ((lane - u0) & 7) * 4);
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            if (lane == u0 + u) {
-              mine = d;
-              my_y = yy[u];
-            }
-          }
+          if (lane - u0 < 8u) mine = d;
         }
       }
       uint32_t c = cb + lane;

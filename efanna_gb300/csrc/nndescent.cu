@@ -405,122 +405,175 @@ __global__ void bound_kernel(uint64_t n, uint32_t P, const float* __restrict__ p
   bound[t] = r > w ? r : w;
 }
 
-// One warp per node i, nodes taken from a shared counter as warps come free (nodes' pair counts
-// differ by an order of magnitude, so fixed assignment leaves most warps of a block idle behind
-// its longest node).  Pass 0: distances of all its pairs (stored) and record counts per target.
-// Pass 1: records written from the stored distances.
+// The record side of one join pair (a lane's pair): x is the list entry being joined, y the
+// candidate, my_new whether y comes from the new list, slot its pairdist index.  Pass 0 stores the
+// distance and counts the records per target; pass 1 reads it back and writes the records.
+// Returns whether side 0 dropped a candidate that a rank below check_k could have needed.
 template <int PASS>
-__global__ void __launch_bounds__(256, 4) join_kernel(const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P,
-                            uint32_t check_k, const uint32_t* __restrict__ new_ids,
-                            const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids,
-                            const uint32_t* __restrict__ old_cnt, const uint64_t* __restrict__ pair_off,
-                            const float* __restrict__ bound, float* __restrict__ pairdist,
-                            uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off,
-                            uint32_t* __restrict__ cursor, uint64_t* __restrict__ rec_key,
-                            uint32_t* __restrict__ rec_aux, uint8_t* __restrict__ found,
-                            uint32_t* __restrict__ next_node) {
+__device__ __forceinline__ bool join_lane_record(uint64_t i, uint32_t x, uint32_t y, bool my_new, float mine,
+                                                 uint64_t slot, uint32_t P, uint32_t check_k,
+                                                 const float* __restrict__ bound, float* __restrict__ pairdist,
+                                                 uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off,
+                                                 uint32_t* __restrict__ cursor, uint64_t* __restrict__ rec_key,
+                                                 uint32_t* __restrict__ rec_aux) {
+  const bool same = my_new && y == x;  // equal ids: no pair
+  if (PASS == 0) pairdist[slot] = same ? __int_as_float(0x7fc00000) : mine;
+  else mine = pairdist[slot];
+  if (same) return false;
+  uint32_t a = x, b = y;
+  if (my_new && b < a) {
+    a = y;
+    b = x;
+  }
+  bool drop = false;
+  // side 0: candidate b into node a (its rank feeds found); side 1: a into b
+  if (mine <= bound[a]) {
+    if (PASS == 0) atomicAdd(&cnt[a], 1u);
+    else {
+      uint32_t pos = atomicAdd(&cursor[a], 1u);
+      rec_key[rec_off[a] + pos] = pack_key(mine, b);
+      rec_aux[rec_off[a] + pos] = (uint32_t)(i << 1);
+    }
+  } else if (P < check_k) {
+    drop = true;
+  }
+  if (mine <= bound[b]) {
+    if (PASS == 0) atomicAdd(&cnt[b], 1u);
+    else {
+      uint32_t pos = atomicAdd(&cursor[b], 1u);
+      rec_key[rec_off[b] + pos] = pack_key(mine, a);
+      rec_aux[rec_off[b] + pos] = (uint32_t)(i << 1) | 1u;
+    }
+  }
+  return drop;
+}
+
+// pairdist index of node i's pair (new entry p, candidate c): the pairs of p' < p come first.
+__device__ __forceinline__ uint64_t join_slot(uint64_t po, uint32_t nn, uint32_t no, uint32_t p, uint32_t c) {
+  uint64_t sp = p == 0 ? 0 : (uint64_t)p * (nn - 1) - (uint64_t)p * (p - 1) / 2 + (uint64_t)p * no;
+  return po + sp + c;
+}
+
+// Join pass 0: the distances of node i's pairs, stored, and record counts per target.  One warp
+// per node, nodes taken from a shared counter as warps come free (pair counts differ by an order
+// of magnitude, so a fixed assignment leaves most warps of a block idle behind its longest node).
+// New entries are taken two at a time: x0 = new[p] pairs with Y = new[p+1..] + old, x1 = new[p+1]
+// with Y[1..], so every candidate row loaded serves both; four rows per pass, the 2 x 4 sums
+// reduced together.
+__global__ void __launch_bounds__(256, 4) join_dist_kernel(
+    const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P, uint32_t check_k,
+    const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids,
+    const uint32_t* __restrict__ old_cnt, const uint64_t* __restrict__ pair_off, const float* __restrict__ bound,
+    float* __restrict__ pairdist, uint32_t* __restrict__ cnt, uint8_t* __restrict__ found,
+    uint32_t* __restrict__ next_node) {
   const uint32_t lane = threadIdx.x & 31;
   for (;;) {
-  uint32_t ii = 0;
-  if (lane == 0) ii = atomicAdd(next_node, 1u);
-  const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
-  if (i >= n) return;
-  uint32_t nn = new_cnt[i], no = old_cnt[i];
-  if (nn == 0) continue;
-  const uint32_t* nw = new_ids + i * cap;
-  const uint32_t* od = old_ids + i * cap;
-  uint64_t po = pair_off[i];
-  bool found_drop = false;
-  for (uint32_t p = 0; p < nn; ++p) {
-    uint32_t x = nw[p];
-    uint32_t m = (nn - 1 - p) + no;
-    for (uint32_t cb = 0; cb < m; cb += 32) {
-      uint32_t cm = min(32u, m - cb);
-      float mine = 0.f;
-      uint32_t my_y = 0;
-      bool my_new = false;
-      if (PASS == 0) {
-        // lane l's candidate (position cb + l; the last one repeated past cm), loaded once per chunk
-        // and handed to the passes by shuffles
+    uint32_t ii = 0;
+    if (lane == 0) ii = atomicAdd(next_node, 1u);
+    const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
+    if (i >= n) return;
+    const uint32_t nn = new_cnt[i], no = old_cnt[i];
+    if (nn == 0) continue;
+    const uint32_t* nw = new_ids + i * cap;
+    const uint32_t* od = old_ids + i * cap;
+    const uint64_t po = pair_off[i];
+    bool found_drop = false;
+    for (uint32_t p = 0; p < nn; p += 2) {
+      const bool two = p + 1 < nn;
+      const uint32_t x0 = nw[p], x1 = two ? nw[p + 1] : x0;
+      const uint32_t nl = nn - 1 - p;  // new-list candidates of x0
+      const uint32_t m = nl + no;      // Y positions (x1 takes positions 1..m-1)
+      const float4* r0 = reinterpret_cast<const float4*>(base) + (uint64_t)x0 * ld4;
+      const float4* r1 = reinterpret_cast<const float4*>(base) + (uint64_t)x1 * ld4;
+      for (uint32_t cb = 0; cb < m; cb += 32) {
+        const uint32_t cm = min(32u, m - cb);
+        // lane l's candidate (position cb + l; the last one repeated past cm), loaded once per
+        // chunk and handed to the passes by shuffles
         const uint32_t cl = cb + min(lane, cm - 1);
-        const uint32_t cand = cl < nn - 1 - p ? nw[p + 1 + cl] : od[cl - (nn - 1 - p)];
-        my_y = cand;
-        const float4* rx = reinterpret_cast<const float4*>(base) + (uint64_t)x * ld4;
-        // 8 rows in flight per lane
-        for (uint32_t u0 = 0; u0 < cm; u0 += 8) {
-          float acc[8];
-          const float4* ry[8];
+        const uint32_t cand = cl < nl ? nw[p + 1 + cl] : od[cl - nl];
+        float mine0 = 0.f, mine1 = 0.f;
+        for (uint32_t u0 = 0; u0 < cm; u0 += 4) {
+          float acc[8];  // [0..4): x0 against rows u0..u0+3, [4..8): x1 against them
+          const float4* ry[4];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < 4; ++u) {
             uint32_t yu = __shfl_sync(0xffffffffu, cand, min(u0 + u, cm - 1));
             ry[u] = reinterpret_cast<const float4*>(base) + (uint64_t)yu * ld4;
             acc[u] = 0.f;
+            acc[u + 4] = 0.f;
           }
           for (uint32_t c4 = lane; c4 < ld4; c4 += 32) {
-            float4 xv = __ldg(rx + c4);
-            float4 yv[8];
+            const float4 a = __ldg(r0 + c4), b = __ldg(r1 + c4);
+            float4 yv[4];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) yv[u] = __ldg(ry[u] + c4);
+            for (int u = 0; u < 4; ++u) yv[u] = __ldg(ry[u] + c4);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              float d0 = xv.x - yv[u].x, d1 = xv.y - yv[u].y, d2 = xv.z - yv[u].z, d3 = xv.w - yv[u].w;
+            for (int u = 0; u < 4; ++u) {
+              float d0 = a.x - yv[u].x, d1 = a.y - yv[u].y, d2 = a.z - yv[u].z, d3 = a.w - yv[u].w;
               acc[u] += d0 * d0;
               acc[u] += d1 * d1;
               acc[u] += d2 * d2;
               acc[u] += d3 * d3;
+              float e0 = b.x - yv[u].x, e1 = b.y - yv[u].y, e2 = b.z - yv[u].z, e3 = b.w - yv[u].w;
+              acc[u + 4] += e0 * e0;
+              acc[u + 4] += e1 * e1;
+              acc[u + 4] += e2 * e2;
+              acc[u + 4] += e3 * e3;
             }
           }
-          // the eight row sums reduced together (lanes 4r .. 4r+3 end with row r's), then row
-          // u's sum moves to lane u0 + u
-          float tot = reduce8_rows(acc, lane);
-          float d = __shfl_sync(0xffffffffu, tot, ((lane - u0) & 7) * 4);
-          if (lane - u0 < 8u) mine = d;
+          // lanes 4r .. 4r+3 end with sum r: r < 4 x0's row u0+r, r >= 4 x1's row u0+r-4; row
+          // u's sums move to lane u0 + u
+          const float tot = reduce8_rows(acc, lane);
+          const uint32_t u = (lane - u0) & 3;
+          const float d0 = __shfl_sync(0xffffffffu, tot, u * 4), d1 = __shfl_sync(0xffffffffu, tot, (u + 4) * 4);
+          if (lane - u0 < 4u) {
+            mine0 = d0;
+            mine1 = d1;
+          }
         }
-      }
-      uint32_t c = cb + lane;
-      if (lane < cm) {
-        my_new = c < nn - 1 - p;
-        if (PASS == 1) my_y = my_new ? nw[p + 1 + c] : od[c - (nn - 1 - p)];
-        // slot = sum_{p' < p} ((nn - 1 - p') + no) + c
-        uint64_t sp = (uint64_t)p * (nn - 1) - (uint64_t)p * (p - 1) / 2 + (uint64_t)p * no;
-        if (p == 0) sp = 0;
-        uint64_t slot = po + sp + c;
-        if (PASS == 0) {
-          if (my_new && my_y == x) mine = __int_as_float(0x7fc00000);  // equal ids: no pair
-          pairdist[slot] = mine;
-        } else {
-          mine = pairdist[slot];
-        }
-        if (!(my_new && my_y == x)) {
-          uint32_t a = x, b = my_y;
-          if (my_new && b < a) {
-            a = my_y;
-            b = x;
-          }
-          // side 0: candidate b into node a (its rank feeds found); side 1: a into b
-          if (mine <= bound[a]) {
-            if (PASS == 0) atomicAdd(&cnt[a], 1u);
-            else {
-              uint32_t pos = atomicAdd(&cursor[a], 1u);
-              rec_key[rec_off[a] + pos] = pack_key(mine, b);
-              rec_aux[rec_off[a] + pos] = (uint32_t)(i << 1);
-            }
-          } else if (P < check_k) {
-            found_drop = true;
-          }
-          if (mine <= bound[b]) {
-            if (PASS == 0) atomicAdd(&cnt[b], 1u);
-            else {
-              uint32_t pos = atomicAdd(&cursor[b], 1u);
-              rec_key[rec_off[b] + pos] = pack_key(mine, a);
-              rec_aux[rec_off[b] + pos] = (uint32_t)(i << 1) | 1u;
-            }
-          }
+        const uint32_t c = cb + lane;
+        if (lane < cm) {
+          const bool my_new = c < nl;
+          found_drop |= join_lane_record<0>(i, x0, cand, my_new, mine0, join_slot(po, nn, no, p, c), P, check_k,
+                                            bound, pairdist, cnt, nullptr, nullptr, nullptr, nullptr);
+          if (two && c >= 1)  // x1's candidate c - 1 (new exactly when x0's candidate c is)
+            found_drop |= join_lane_record<0>(i, x1, cand, my_new, mine1, join_slot(po, nn, no, p + 1, c - 1), P,
+                                              check_k, bound, pairdist, cnt, nullptr, nullptr, nullptr, nullptr);
         }
       }
     }
+    if (__any_sync(0xffffffffu, found_drop) && lane == 0) found[i] = 1;
   }
-  if (PASS == 0 && __any_sync(0xffffffffu, found_drop) && lane == 0) found[i] = 1;
+}
+
+// Join pass 1: node i's records written from the stored distances (warps take nodes from a
+// shared counter, as in pass 0).
+__global__ void __launch_bounds__(256, 4) join_records_kernel(
+    uint64_t n, uint32_t cap, uint32_t P, uint32_t check_k, const uint32_t* __restrict__ new_ids,
+    const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids, const uint32_t* __restrict__ old_cnt,
+    const uint64_t* __restrict__ pair_off, const float* __restrict__ bound, float* __restrict__ pairdist,
+    const uint64_t* __restrict__ rec_off, uint32_t* __restrict__ cursor, uint64_t* __restrict__ rec_key,
+    uint32_t* __restrict__ rec_aux, uint32_t* __restrict__ next_node) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t ii = 0;
+    if (lane == 0) ii = atomicAdd(next_node, 1u);
+    const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
+    if (i >= n) return;
+    const uint32_t nn = new_cnt[i], no = old_cnt[i];
+    if (nn == 0) continue;
+    const uint32_t* nw = new_ids + i * cap;
+    const uint32_t* od = old_ids + i * cap;
+    const uint64_t po = pair_off[i];
+    for (uint32_t p = 0; p < nn; ++p) {
+      const uint32_t x = nw[p], nl = nn - 1 - p, m = nl + no;
+      for (uint32_t c = lane; c < m; c += 32) {
+        const bool my_new = c < nl;
+        const uint32_t y = my_new ? nw[p + 1 + c] : od[c - nl];
+        join_lane_record<1>(i, x, y, my_new, 0.f, join_slot(po, nn, no, p, c), P, check_k, bound, pairdist, nullptr,
+                            rec_off, cursor, rec_key, rec_aux);
+      }
+    }
   }
 }
 
@@ -959,13 +1012,13 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   int sms = 152, per0 = 1, per1 = 1, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, join_kernel<0>, 256, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, join_kernel<1>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, join_dist_kernel, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, join_records_kernel, 256, 0);
   const unsigned jgrid0 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per0, 1));
   const unsigned jgrid1 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per1, 1));
-  join_kernel<0><<<jgrid0, 256, 0, s>>>(
-      idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p,
-      bound.p, S.pairdist.p, S.cnt.p, nullptr, nullptr, nullptr, nullptr, S.found.p, jctr.p);
+  join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
+                                          S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
+                                          S.found.p, jctr.p);
   EFG_CUDA(cudaGetLastError());
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, tmp64.p, n);
   EFG_TRY(device_scan<uint64_t>(tmp64.p, n, S.rec_off64.p, S.scan64.p, s));
@@ -974,9 +1027,9 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaStreamSynchronize(s));
   EFG_TRY(S.rec_key.reserve(nrec + 1));
   EFG_TRY(S.rec_aux.reserve(nrec + 1));
-  join_kernel<1><<<jgrid1, 256, 0, s>>>(
-      idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p,
-      bound.p, S.pairdist.p, S.cnt.p, S.rec_off64.p, S.cursor.p, S.rec_key.p, S.rec_aux.p, S.found.p, jctr.p + 1);
+  join_records_kernel<<<jgrid1, 256, 0, s>>>(n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p,
+                                             S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.rec_off64.p,
+                                             S.cursor.p, S.rec_key.p, S.rec_aux.p, jctr.p + 1);
   EFG_CUDA(cudaGetLastError());
   if (S.P <= 32)
     merge_kernel<1><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,

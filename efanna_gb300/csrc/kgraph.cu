@@ -108,11 +108,11 @@ __device__ __forceinline__ float warp_row_dists(const float4* qv, uint32_t ld4, 
         acc[u] += d3 * d3;
       }
     }
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      float t = warp_sum(acc[u]);
-      if (lane == u0 + u) mine = t;
-    }
+    // the eight sums reduced together (lanes 4r .. 4r+3 end with row r's), then row u's sum
+    // moves to lane u0 + u
+    const float tot = reduce8_rows(acc, lane);
+    const float t = __shfl_sync(FULL, tot, ((lane - u0) & 7) * 4);
+    if (lane - u0 < 8u) mine = t;
   }
   return mine;
 }
@@ -222,18 +222,20 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
           uint32_t lb = lane < cnt ? lower_bound_keys(list, L, dk) : L;
           uint32_t newL = min(c.C, L + cnt);
           uint32_t first = __shfl_sync(FULL, lb, 0);
-          for (int32_t hi = (int32_t)L; hi > (int32_t)first; hi -= 32) {  // old entries move right
-            int32_t i = hi - 32 + (int32_t)lane;
-            bool act = i >= (int32_t)first;
-            uint64_t v = act ? list[i] : 0;
-            uint32_t shift = 0;
-            for (uint32_t j = 0; j < cnt; ++j) {
-              uint32_t lbj = __shfl_sync(FULL, lb, j);
-              shift += (act && lbj <= (uint32_t)i) ? 1u : 0u;
+          // old entries move right: those in [lb_j, lb_{j+1}) (lb_cnt = L) by j + 1, the highest
+          // segment first, each copied from its top down (reads before writes within a round)
+          for (int32_t j = (int32_t)cnt - 1; j >= 0; --j) {
+            const uint32_t s_lo = __shfl_sync(FULL, lb, j);
+            const uint32_t s_hi = __shfl_sync(FULL, lb, j + 1 < (int32_t)cnt ? j + 1 : j);
+            const uint32_t top = j + 1 < (int32_t)cnt ? s_hi : L;
+            for (int32_t hi = (int32_t)top; hi > (int32_t)s_lo; hi -= 32) {
+              int32_t i = hi - 32 + (int32_t)lane;
+              bool act = i >= (int32_t)s_lo;
+              uint64_t v = act ? list[i] : 0;
+              __syncwarp();
+              if (act && (uint32_t)i + j + 1 < newL) list[i + j + 1] = v;
+              __syncwarp();
             }
-            __syncwarp();
-            if (act && (uint32_t)i + shift < newL) list[i + shift] = v;
-            __syncwarp();
           }
           if (lane < cnt && lb + lane < newL) list[lb + lane] = dk;
           __syncwarp();

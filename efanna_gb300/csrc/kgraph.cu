@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
     const float* __restrict__ base, uint32_t dim, uint32_t ld, const uint64_t* __restrict__ gptr,
     const uint32_t* __restrict__ gids, const float* __restrict__ queries, uint64_t nq, uint64_t qld,
     const uint64_t* __restrict__ keys, KgCfg c, int32_t* __restrict__ out, uint32_t* __restrict__ bits,
-    unsigned long long* __restrict__ stats) {
+    unsigned long long* __restrict__ stats, uint32_t* __restrict__ next_query) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   unsigned char* ws = smem + (size_t)wib * c.warp_bytes;
@@ -129,11 +129,16 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
   uint64_t* list = reinterpret_cast<uint64_t*>(ws + c.o_list);
   uint64_t* res = reinterpret_cast<uint64_t*>(ws + c.o_res);
   uint64_t* res2 = reinterpret_cast<uint64_t*>(ws + c.o_res2);
-  const uint64_t gw = (uint64_t)blockIdx.x * KG_WARPS + wib, nw = (uint64_t)gridDim.x * KG_WARPS;
+  const uint64_t gw = (uint64_t)blockIdx.x * KG_WARPS + wib;
   uint32_t* vis = bits + gw * c.words;
   unsigned long long evals = 0, expanded = 0;
 
-  for (uint64_t q = gw; q < nq; q += nw) {
+  // queries taken from a shared counter as warps come free (their expansion counts differ)
+  for (;;) {
+    uint32_t qq = 0;
+    if (lane == 0) qq = atomicAdd(next_query, 1u);
+    const uint64_t q = __shfl_sync(FULL, qq, 0);
+    if (q >= nq) break;
     const float* qrow = queries + q * qld;
     for (uint32_t i = lane; i < c.ld4; i += 32) {
       uint32_t e = 4 * i;
@@ -358,6 +363,10 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   int launches = 0, rc = EFG_OK;
+  const uint64_t nchunks = (nq + chunk - 1) / chunk;
+  LocalBuf<uint32_t> qctr;  // one query counter per chunk launch
+  EFG_TRY(qctr.reserve(nchunks));
+  EFG_CUDA(cudaMemsetAsync(qctr.p, 0, nchunks * 4, s));
   for (uint64_t q0 = 0; q0 < nq && rc == EFG_OK; q0 += chunk) {
     uint64_t m = std::min(chunk, nq - q0);
     int l = 0;
@@ -377,7 +386,7 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
     kgraph_kernel<<<(unsigned)grid, KG_WARPS * 32, smem, s>>>(idx->d_base, idx->dim, idx->ld, idx->graph.ptr.p,
                                                               idx->graph.ids.p, d_q + q0 * qld, m, qld,
                                                               idx->kg_keys.p, kc, d_out + q0 * k, idx->kg_bits.p,
-                                                              idx->eval_counter.p);
+                                                              idx->eval_counter.p, qctr.p + q0 / chunk);
     cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) rc = fail(EFG_ERR_CUDA, std::string("kgraph launch: ") + cudaGetErrorString(le));
     ++launches;

@@ -168,35 +168,54 @@ __global__ void __launch_bounds__(BF_THREADS) bf_chunk_kernel(const float* __res
     }
   };
 
-  for (uint64_t rb = r0; rb < r1; rb += BF_THREADS) {
-    uint64_t r = rb + threadIdx.x;
-    if (r < r1) {
-      float acc[BF_QB];
+  // two rows per thread per step: every query chunk read from shared memory serves both
+  for (uint64_t rb = r0; rb < r1; rb += 2 * BF_THREADS) {
+    const uint64_t ra = rb + threadIdx.x, rc = ra + BF_THREADS;
+    if (ra < r1) {
+      const bool two = rc < r1;
+      float acc0[BF_QB], acc1[BF_QB];
 #pragma unroll
-      for (int j = 0; j < BF_QB; ++j) acc[j] = 0.f;
-      const float4* row = reinterpret_cast<const float4*>(base + r * ld);
+      for (int j = 0; j < BF_QB; ++j) {
+        acc0[j] = 0.f;
+        acc1[j] = 0.f;
+      }
+      const float4* row0 = reinterpret_cast<const float4*>(base + ra * ld);
+      const float4* row1 = reinterpret_cast<const float4*>(base + (two ? rc : ra) * ld);
       for (uint32_t c = 0; c < ld4; ++c) {
-        float4 x = __ldg(row + c);
+        float4 x0 = __ldg(row0 + c), x1 = __ldg(row1 + c);
         uint32_t e = c << 2;
         if (e + 4 > dim) {
-          if (e + 2 > dim) x.y = 0.f;
-          if (e + 3 > dim) x.z = 0.f;
-          x.w = 0.f;
+          if (e + 2 > dim) x0.y = x1.y = 0.f;
+          if (e + 3 > dim) x0.z = x1.z = 0.f;
+          x0.w = x1.w = 0.f;
         }
 #pragma unroll
         for (int j = 0; j < BF_QB; ++j) {
           float4 y = qt[j * ld4 + c];
-          float d0 = x.x - y.x, d1 = x.y - y.y, d2 = x.z - y.z, d3 = x.w - y.w;
-          acc[j] += d0 * d0;
-          acc[j] += d1 * d1;
-          acc[j] += d2 * d2;
-          acc[j] += d3 * d3;
+          float d0 = x0.x - y.x, d1 = x0.y - y.y, d2 = x0.z - y.z, d3 = x0.w - y.w;
+          acc0[j] += d0 * d0;
+          acc0[j] += d1 * d1;
+          acc0[j] += d2 * d2;
+          acc0[j] += d3 * d3;
+          float e0 = x1.x - y.x, e1 = x1.y - y.y, e2 = x1.z - y.z, e3 = x1.w - y.w;
+          acc1[j] += e0 * e0;
+          acc1[j] += e1 * e1;
+          acc1[j] += e2 * e2;
+          acc1[j] += e3 * e3;
         }
       }
 #pragma unroll
       for (int j = 0; j < BF_QB; ++j) {
-        if ((uint32_t)j < nqb && !(exclude_self && r == first_row + q0 + j)) {
-          uint64_t key = pack_key(acc[j], (uint32_t)r);
+        if ((uint32_t)j >= nqb) continue;
+        if (!(exclude_self && ra == first_row + q0 + j)) {
+          uint64_t key = pack_key(acc0[j], (uint32_t)ra);
+          if (key < thr[j]) {
+            uint32_t pos = atomicAdd(&cnt[j], 1u);
+            if (pos < BF_CAP) cand[(size_t)j * BF_CAP + pos] = key;
+          }
+        }
+        if (two && !(exclude_self && rc == first_row + q0 + j)) {
+          uint64_t key = pack_key(acc1[j], (uint32_t)rc);
           if (key < thr[j]) {
             uint32_t pos = atomicAdd(&cnt[j], 1u);
             if (pos < BF_CAP) cand[(size_t)j * BF_CAP + pos] = key;
@@ -207,7 +226,7 @@ __global__ void __launch_bounds__(BF_THREADS) bf_chunk_kernel(const float* __res
     __syncthreads();
     if (threadIdx.x == 0) {
       int np = 0;
-      for (int j = 0; j < BF_QB; ++j) np |= cnt[j] + BF_THREADS > BF_CAP;
+      for (int j = 0; j < BF_QB; ++j) np |= cnt[j] + 2 * BF_THREADS > BF_CAP;
       need_prune = np;
     }
     __syncthreads();

@@ -129,98 +129,107 @@ __global__ void min_leaf_level_kernel(TreeView tv, uint64_t nnodes, uint32_t tre
 // keeps each task's point, leaf and distances (maxl per task), and merge_emit_kernel writes the
 // records from them instead of a second routing pass.
 template <int PASS>
-__global__ void __launch_bounds__(256, 4) merge_route_kernel(const float* __restrict__ base, uint32_t ld4, TreeView tv,
+__global__ void __launch_bounds__(256, 3) merge_route_kernel(const float* __restrict__ base, uint32_t ld4, TreeView tv,
                                    const uint64_t* __restrict__ task_off, uint64_t nnodes, uint64_t ntasks,
                                    uint32_t* __restrict__ cnt, const uint64_t* __restrict__ off,
                                    uint32_t* __restrict__ cursor, uint64_t* __restrict__ keys,
                                    unsigned long long* __restrict__ ndist, uint32_t* __restrict__ task_p,
                                    int32_t* __restrict__ task_leaf, float* __restrict__ task_d, uint32_t maxl) {
-  uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  uint32_t lane = threadIdx.x & 31;
+  // a warp routes 32 consecutive tasks at once, one per lane (search and descent are chains of
+  // dependent loads: the lanes run theirs side by side), then the whole warp computes each task's
+  // leaf distances in turn
+  const uint64_t gwarp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
   unsigned long long local = 0;
   const float* fb = base;
-  for (; w < ntasks; w += nw) {
-    // node owning task w: last v with task_off[v] <= w, searched by the whole warp (32 probes a
-    // round, so about five dependent rounds instead of a load per halving)
-    uint64_t lo = 0, hi = nnodes;
-    while (hi - lo > 32) {
-      uint64_t step = (hi - lo + 31) / 32;
-      uint64_t probe = lo + (uint64_t)lane * step;
-      bool le = probe < hi && task_off[probe] <= w;  // true for a prefix of the lanes (lane 0 always)
-      uint32_t k = 31 - __clz(__ballot_sync(0xffffffffu, le));
-      lo += (uint64_t)k * step;
-      hi = min(hi, lo + step);
-    }
-    {
-      uint64_t probe = lo + lane;
-      bool le = probe < hi && task_off[probe] <= w;
-      lo += 31 - __clz(__ballot_sync(0xffffffffu, le));
-    }
-    uint64_t v = lo;
-    int32_t L = tv.left[v], R = tv.right[v];
-    uint64_t nl = tv.end[L] - tv.start[L], nr = tv.end[R] - tv.start[R];
-    int32_t root = nl < nr ? R : L;
-    int32_t small = nl < nr ? L : R;
-    uint64_t t = (uint64_t)tv.tree[v];
-    const uint32_t* ll = tv.leaves + t * tv.n;
-    uint32_t p = ll[tv.start[small] + (w - task_off[v])];
-    int32_t cur = root;
-    DNode nd = tv.nodes[cur];
-    while (nd.left >= 0) {
-      float x = __ldg(fb + (uint64_t)p * (ld4 * 4) + nd.div_dim);
-      cur = x < nd.div_val ? nd.left : nd.right;
-      nd = tv.nodes[cur];
-    }
-    uint32_t ls = (uint32_t)(-(nd.left + 1)), le = (uint32_t)nd.right;
-    if (PASS == 0 && task_d && lane == 0) {
-      task_p[w] = p;
-      task_leaf[w] = cur;
-    }
-    const float4* rp = reinterpret_cast<const float4*>(base) + (uint64_t)p * ld4;
-    for (uint32_t i0 = ls; i0 < le; i0 += 8) {  // eight leaf points at a time, their loads in flight together
-      const uint32_t cnt8 = min(8u, le - i0);
-      uint32_t qq[8];
-      float acc[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        qq[u] = ll[i0 + min((uint32_t)u, cnt8 - 1)];
-        acc[u] = 0.f;
+  for (uint64_t wb = gwarp * 32; wb < ntasks; wb += nwarps * 32) {
+    const uint64_t myw = wb + lane;
+    uint32_t myp = 0, mls = 0, mle = 0;
+    int32_t mleaf = 0;
+    uint64_t mt = 0;
+    if (myw < ntasks) {
+      // node owning task myw: last v with task_off[v] <= myw
+      uint64_t lo = 0, hi = nnodes;
+      while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (task_off[mid] <= myw) lo = mid;
+        else hi = mid;
       }
-      for (uint32_t c = lane; c < ld4; c += 32) {
-        float4 y = __ldg(rp + c);
-        float4 x[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x[u] = __ldg(reinterpret_cast<const float4*>(base) + (uint64_t)qq[u] * ld4 + c);
+      const uint64_t v = lo;
+      int32_t L = tv.left[v], R = tv.right[v];
+      uint64_t nl = tv.end[L] - tv.start[L], nr = tv.end[R] - tv.start[R];
+      int32_t cur = nl < nr ? R : L;
+      int32_t small = nl < nr ? L : R;
+      mt = (uint64_t)tv.tree[v];
+      myp = tv.leaves[mt * tv.n + tv.start[small] + (myw - task_off[v])];
+      DNode nd = tv.nodes[cur];
+      while (nd.left >= 0) {
+        float x = __ldg(fb + (uint64_t)myp * (ld4 * 4) + nd.div_dim);
+        cur = x < nd.div_val ? nd.left : nd.right;
+        nd = tv.nodes[cur];
+      }
+      mleaf = cur;
+      mls = (uint32_t)(-(nd.left + 1));
+      mle = (uint32_t)nd.right;
+      if (PASS == 0 && task_d) {
+        task_p[myw] = myp;
+        task_leaf[myw] = cur;
+      }
+    }
+    const uint32_t ntask = ntasks - wb < 32 ? (uint32_t)(ntasks - wb) : 32u;
+    for (uint32_t j = 0; j < ntask; ++j) {
+      const uint64_t w = wb + j;
+      const uint32_t p = __shfl_sync(0xffffffffu, myp, j);
+      const uint32_t ls = __shfl_sync(0xffffffffu, mls, j), le = __shfl_sync(0xffffffffu, mle, j);
+      const uint64_t t = __shfl_sync(0xffffffffu, mt, j);
+      const uint32_t* ll = tv.leaves + t * tv.n;
+      const float4* rp = reinterpret_cast<const float4*>(base) + (uint64_t)p * ld4;
+      for (uint32_t i0 = ls; i0 < le; i0 += 8) {  // eight leaf points at a time, their loads in flight together
+        const uint32_t cnt8 = min(8u, le - i0);
+        uint32_t qq[8];
+        float acc[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          float d0 = x[u].x - y.x, d1 = x[u].y - y.y, d2 = x[u].z - y.z, d3 = x[u].w - y.w;
-          acc[u] += d0 * d0;
-          acc[u] += d1 * d1;
-          acc[u] += d2 * d2;
-          acc[u] += d3 * d3;
+          qq[u] = ll[i0 + min((uint32_t)u, cnt8 - 1)];
+          acc[u] = 0.f;
         }
-      }
-      const float d = reduce8_rows(acc, lane);  // lanes 4r .. 4r+3: leaf point r's distance
-      const uint32_t r = lane >> 2;
-      uint32_t q = qq[0];
+        for (uint32_t c = lane; c < ld4; c += 32) {
+          float4 y = __ldg(rp + c);
+          float4 x[8];
 #pragma unroll
-      for (int u = 1; u < 8; ++u)
-        if (r == (uint32_t)u) q = qq[u];
-      local += cnt8;
-      if ((lane & 3) == 0 && r < cnt8) {
-        if (PASS == 0) {
-          if (task_d) task_d[w * maxl + (i0 - ls) + r] = d;
-          atomicAdd(&cnt[q], 1u);
-          atomicAdd(&cnt[p], 1u);
-        } else {
-          uint32_t a = atomicAdd(&cursor[q], 1u);
-          keys[off[q] + a] = pack_key(d, p);
-          uint32_t b = atomicAdd(&cursor[p], 1u);
-          keys[off[p] + b] = pack_key(d, q);
+          for (int u = 0; u < 8; ++u) x[u] = __ldg(reinterpret_cast<const float4*>(base) + (uint64_t)qq[u] * ld4 + c);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            float d0 = x[u].x - y.x, d1 = x[u].y - y.y, d2 = x[u].z - y.z, d3 = x[u].w - y.w;
+            acc[u] += d0 * d0;
+            acc[u] += d1 * d1;
+            acc[u] += d2 * d2;
+            acc[u] += d3 * d3;
+          }
+        }
+        const float d = reduce8_rows(acc, lane);  // lanes 4r .. 4r+3: leaf point r's distance
+        const uint32_t r = lane >> 2;
+        uint32_t q = qq[0];
+#pragma unroll
+        for (int u = 1; u < 8; ++u)
+          if (r == (uint32_t)u) q = qq[u];
+        local += cnt8;
+        if ((lane & 3) == 0 && r < cnt8) {
+          if (PASS == 0) {
+            if (task_d) task_d[w * maxl + (i0 - ls) + r] = d;
+            atomicAdd(&cnt[q], 1u);
+            atomicAdd(&cnt[p], 1u);
+          } else {
+            uint32_t a = atomicAdd(&cursor[q], 1u);
+            keys[off[q] + a] = pack_key(d, p);
+            uint32_t b = atomicAdd(&cursor[p], 1u);
+            keys[off[p] + b] = pack_key(d, q);
+          }
         }
       }
     }
+    (void)mleaf;
   }
   if (PASS == 0 && lane == 0 && local) atomicAdd(ndist, local);
 }

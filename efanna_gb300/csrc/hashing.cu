@@ -258,6 +258,7 @@ int efg_hash_seeds_device(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_
 
 int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64_t nq, uint64_t row_stride,
                            const uint64_t* d_qcodes, uint64_t qcode_stride, uint32_t k, int32_t* d_out, void* stream) {
+  NvtxRange range("efg: hashing-seeded search");
   if (!idx || !h || ((!d_q || !d_qcodes || !d_out) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (h->idx != idx) return fail(EFG_ERR_ARG, "the hash tables belong to another index");
   if (row_stride < idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");

@@ -2,6 +2,8 @@
 #pragma once
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace efg {
@@ -30,6 +32,29 @@ struct DevBuf {
     p = nullptr;
     cap = 0;
   }
+};
+
+// An NVTX range over a scope (named phases for Nsight Systems / Nsight Compute; free when no tool
+// is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+// CUDA events owned by a scope (destroyed on every return path).
+template <int N>
+struct ScopedEvents {
+  cudaEvent_t e[N];
+  ScopedEvents() {
+    for (auto& x : e) cudaEventCreate(&x);
+  }
+  ~ScopedEvents() {
+    for (auto& x : e) cudaEventDestroy(x);
+  }
+  ScopedEvents(const ScopedEvents&) = delete;
+  ScopedEvents& operator=(const ScopedEvents&) = delete;
 };
 
 // A function-local device buffer: freed when it goes out of scope (also on early error returns).

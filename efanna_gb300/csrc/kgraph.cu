@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(KG_WARPS * 32, 6) kgraph_kernel(
 
 int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                          cudaStream_t s, bool count_evals, const KgSeedSource* hs) {
+  NvtxRange range("efg: kgraph search");
   SearchParams& sp = idx->sp;
   if (hs) {  // pools from the hash tables: no trees needed
     if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph: build or load a graph before searching");

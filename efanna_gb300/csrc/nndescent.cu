@@ -1093,16 +1093,24 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
 }
 
 int build_graph_device(efg_index* idx) {
+  NvtxRange range("efg: build graph");
   cudaStream_t s = idx->stream;
   idx->bstats = efg_build_stats{};
   idx->graph.release();
-  cudaEvent_t ev[4];
-  for (auto& e : ev) cudaEventCreate(&e);
+  ScopedEvents<4> evs;
+  cudaEvent_t* ev = evs.e;
   cudaEventRecord(ev[0], s);
-  EFG_TRY(build_forest(idx, idx->bp.trees));
+  {
+    NvtxRange r("efg: build trees");
+    EFG_TRY(build_forest(idx, idx->bp.trees));
+  }
   cudaEventRecord(ev[1], s);
   NNDev S;
-  int rc = nnd_init_device(idx, S);
+  int rc;
+  {
+    NvtxRange r("efg: leaf-merge init");
+    rc = nnd_init_device(idx, S);
+  }
   if (rc != EFG_OK) {
     S.release_all();
     return rc;
@@ -1111,6 +1119,7 @@ int build_graph_device(efg_index* idx) {
   uint64_t pairs = 0, recs = 0;
   for (uint32_t it = 0; it < idx->bp.epochs; ++it) {
     uint64_t p = 0, r = 0;
+    NvtxRange range_it("efg: nn-descent iteration");
     rc = nnd_iterate_device(idx, S, it, &p, &r);
     if (rc != EFG_OK) {
       S.release_all();
@@ -1138,7 +1147,6 @@ int build_graph_device(efg_index* idx) {
   cudaEventElapsedTime(&a, ev[0], ev[1]);
   cudaEventElapsedTime(&b, ev[1], ev[2]);
   cudaEventElapsedTime(&c, ev[2], ev[3]);
-  for (auto& e : ev) cudaEventDestroy(e);
   idx->bstats.trees_ms = a;
   idx->bstats.init_ms = b;
   idx->bstats.refine_ms = c;

@@ -384,6 +384,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
                      bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query, bool use_trees,
                      bool bucket_only) {
+  NvtxRange range("efg: nnexp search");
   const SearchParams& sp = idx->sp;
   efg_query_params lim = lim_in;
   const uint32_t k = lim.k;

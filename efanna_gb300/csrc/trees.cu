@@ -357,9 +357,8 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
   EFG_TRY(next_pos.reserve(2 * cap_act + 1));
   EFG_TRY(tmp32.reserve(scan_tmp_elems<uint32_t>(2 * cap_act) + 1));
 
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  ScopedEvents<2> evs;
+  cudaEvent_t e0 = evs.e[0], e1 = evs.e[1];
   cudaEventRecord(e0, s);
   perm_init_kernel<<<grid_for(total, 256), 256, 0, s>>>(F.leaves.p, owner.p, n, ntrees, seed);
   roots_init_kernel<<<(ntrees + 255) / 256, 256, 0, s>>>(na, ntrees, n);
@@ -432,8 +431,6 @@ int build_forest(efg_index* idx, uint32_t ntrees) {
   EFG_CUDA(cudaStreamSynchronize(s));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   idx->bstats.trees_ms = ms;
   F.ntrees = ntrees;
   F.n = n;

@@ -395,17 +395,50 @@ def measure_batching(E, X, args):
     recall_all = float(np.mean([len(set(r[:k]) & set(g[:k])) / k for r, g, k in zip(res, gts, ks[sub])]))
     limits = (int(p[:, 0].max()), int(p[:, 1].max()), int(p[:, 2].max()), 100)
     plan = idx.search_plan(8192, limits, calib=q[:2048])
+    plan2 = idx.search_plan(8192, limits, calib=q[:2048])  # a second plan: two batches in flight
     out = np.zeros((8192, 100), np.int32)
     for w in range(3):
         plan.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
-    lat, s_ = [], 0
+        plan2.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
+    # one batch in flight: submit, wait, next
+    lat1, s_ = [], 0
+    ids1 = np.zeros((total, 100), np.int32)
     t_all = time.perf_counter()
     for b in sizes:
         t0 = time.perf_counter()
         plan.run(q[s_:s_ + b], p[s_:s_ + b], out[:b])
-        lat.append(time.perf_counter() - t0)
+        lat1.append(time.perf_counter() - t0)
+        ids1[s_:s_ + b] = out[:b]
         s_ += b
+    wall1 = time.perf_counter() - t_all
+    # two batches in flight on two plans (own streams and scratch): batch i is collected just
+    # before batch i + 2 is submitted on the same plan
+    plans, outs = [plan, plan2], [np.zeros((8192, 100), np.int32), np.zeros((8192, 100), np.int32)]
+    pending = [None, None]
+    lat, s_ = [], 0
+    ids2 = np.zeros((total, 100), np.int32)
+
+    def collect(j):
+        off, bs, ts = pending[j]
+        plans[j].collect(outs[j])
+        lat.append(time.perf_counter() - ts)
+        ids2[off:off + bs] = outs[j][:bs]
+        pending[j] = None
+
+    t_all = time.perf_counter()
+    for i, b in enumerate(sizes):
+        j = i % 2
+        if pending[j] is not None:
+            collect(j)
+        ts = time.perf_counter()
+        plans[j].submit(q[s_:s_ + b], p[s_:s_ + b])
+        pending[j] = (s_, b, ts)
+        s_ += b
+    for j in (0, 1):
+        if pending[j] is not None:
+            collect(j)
     wall = time.perf_counter() - t_all
+    same = bool(np.array_equal(ids1, ids2))
     res = {"value": round(total / wall, 1), "unit": "queries/s", "queries": total, "batches": len(sizes),
            "batch_latency_ms": {"p50": round(float(np.percentile(lat, 50)) * 1e3, 3),
                                 "p99": round(float(np.percentile(lat, 99)) * 1e3, 3),
@@ -414,10 +447,16 @@ def measure_batching(E, X, args):
            "recall@k": round(recall_all, 4), "extend_scale_per_k": {str(k): v for k, v in chosen.items()},
            "ladder": ladder,
            "plan_threads": plan.threads, "graph": "K=20 (trees 8, ml 8, iter 8, L 40, check 25, S 10)",
-           "graph_build_s": round(build_s, 3),
-           "form": "per-query k in {1,10,50,100}, pool = U(6,10) x extend; one captured CUDA graph replayed "
-                   "per batch (host queries in, ids out), persistent kernel, autotuned block size"}
+           "graph_build_s": round(build_s, 3), "in_flight": 2,
+           "one_in_flight": {"value": round(total / wall1, 1),
+                             "batch_latency_ms": {"p50": round(float(np.percentile(lat1, 50)) * 1e3, 3),
+                                                  "p99": round(float(np.percentile(lat1, 99)) * 1e3, 3)}},
+           "ids_equal_to_one_in_flight": same,
+           "form": "per-query k in {1,10,50,100}, pool = U(6,10) x extend; captured CUDA graphs replayed per "
+                   "batch (host queries in, ids out) on two plans with their own streams, scratch and pinned "
+                   "staging, two batches in flight; persistent kernel, autotuned block size"}
     plan.close()
+    plan2.close()
     idx.close()
     return res
 

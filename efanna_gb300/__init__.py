@@ -169,6 +169,8 @@ def lib():
         "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
         "efg_knn_search_seeded_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, u32, i32, vp, vp]),
         "efg_search_plan_create": (i32, [vp, u64, C.POINTER(QueryParams), f32p, u64, C.POINTER(vp)]),
+        "efg_search_plan_submit": (i32, [vp, f32p, u64, u64, vp]),
+        "efg_search_plan_collect": (i32, [vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_threads": (i32, [vp]),
         "efg_search_plan_destroy": (None, [vp]),
@@ -399,6 +401,23 @@ class SearchPlan:
         _check(lib().efg_search_plan_run(self._h, _fp(q), q.shape[0], q.shape[1], C.c_void_p(p.ctypes.data),
                                          out.ctypes.data_as(C.POINTER(C.c_int32))))
         return out
+
+    def submit(self, queries: np.ndarray, params) -> int:
+        """Queues a batch without waiting (the rows are staged before this returns); collect()
+        writes its ids.  Returns the batch size."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        p = query_params(params)
+        _check(lib().efg_search_plan_submit(self._h, _fp(q), q.shape[0], q.shape[1], C.c_void_p(p.ctypes.data)))
+        self._pending = q.shape[0]
+        return q.shape[0]
+
+    def collect(self, out: np.ndarray | None = None) -> np.ndarray:
+        n = getattr(self, "_pending", 0)
+        if out is None:
+            out = np.zeros((n, self.limits.k), dtype=np.int32)
+        _check(lib().efg_search_plan_collect(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        self._pending = 0
+        return out[:n]
 
     def close(self):
         if self._h:

@@ -262,15 +262,22 @@ int efg_hash_search(efg_index* idx, efg_hash* h, const float* queries, uint64_t 
 void efg_hash_destroy(efg_hash* h);
 
 /* A search plan: the batched nnexp launch sequence for up to `capacity` queries whose parameters
- * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers.  When
+ * are bounded by *limits, captured once in a CUDA graph over the plan's own device buffers (queries,
+ * parameters, ids and the search's scratch) and replayed on the plan's own stream.  When
  * calibration queries are given (n_calib > 0, host memory, dim floats per row), the plan's
  * autotuner times the 256- and 512-thread kernel builds on them with the limits' parameters and
- * keeps the faster.  efg_search_plan_run copies a batch in (queries, per-query parameters), replays
- * the graph and copies nq rows of limits->k ids out.  A plan belongs to its index: the index must
- * outlive it and must not be searched by other calls while a run is in progress. */
+ * keeps the faster.  efg_search_plan_submit stages a batch (queries, per-query parameters) through
+ * the plan's pinned buffers and queues the copies, the graph and the copy of the ids without
+ * waiting; efg_search_plan_collect waits for that batch and writes its nq rows of limits->k ids;
+ * efg_search_plan_run does both.  Several plans of one index may have batches in flight at once
+ * (one each: a plan's batch is collected before its next submit).  A plan belongs to its index:
+ * the index must outlive it, and creating a plan must not overlap other calls on the index. */
 typedef struct efg_search_plan efg_search_plan;
 int efg_search_plan_create(efg_index* idx, uint64_t capacity, const efg_query_params* limits,
                            const float* calib_queries, uint64_t n_calib, efg_search_plan** out);
+int efg_search_plan_submit(efg_search_plan* plan, const float* queries, uint64_t nq, uint64_t row_stride,
+                           const efg_query_params* params);
+int efg_search_plan_collect(efg_search_plan* plan, int32_t* out_ids);
 int efg_search_plan_run(efg_search_plan* plan, const float* queries, uint64_t nq, uint64_t row_stride,
                         const efg_query_params* params, int32_t* out_ids);
 /* Block size the autotuner chose (256 or 512; 0 when the plan chose by occupancy). */

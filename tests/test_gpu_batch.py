@@ -94,6 +94,37 @@ def test_search_plan_replays(efg, setup, calibrate):
     plan.close()
 
 
+def test_two_plans_in_flight(efg, setup):
+    """Two plans of one index with batches in flight at once (own streams and scratch; a batch
+    larger than a CTA wave so the overflow and migration scratch is exercised too): every batch's
+    rows equal the oracle's; a plan refuses a second submit before its collect."""
+    idx, q, _, oracle = setup
+    plans = [idx.search_plan(128, (6, 1000, 150, 100)), idx.search_plan(128, (6, 1000, 150, 100))]
+    rng = np.random.default_rng(9)
+    batches = []
+    for i in range(6):
+        size = int(rng.integers(1, 129))
+        rows = rng.choice(q.shape[0], size, replace=False)
+        pick, params = _params(size, 100 + i)
+        batches.append((rows, pick, params))
+    pending = [None, None]
+    for i, (rows, pick, params) in enumerate(batches):
+        j = i % 2
+        if pending[j] is not None:
+            r0, p0 = pending[j]
+            _check_rows(plans[j].collect(), p0, oracle(q[r0]))
+        plans[j].submit(q[rows], params)
+        if i == 0:
+            with pytest.raises(efg.EfannaError):
+                plans[0].submit(q[rows], params)
+        pending[j] = (rows, pick)
+    for j in (0, 1):
+        r0, p0 = pending[j]
+        _check_rows(plans[j].collect(), p0, oracle(q[r0]))
+    for pl in plans:
+        pl.close()
+
+
 def test_batch_argument_errors(efg, setup):
     idx, q, _, _ = setup
     with pytest.raises(efg.EfannaError):

@@ -394,12 +394,12 @@ def measure_batching(E, X, args):
     res = idx.knn_search_batch(q[sub], p[sub], 100)
     recall_all = float(np.mean([len(set(r[:k]) & set(g[:k])) / k for r, g, k in zip(res, gts, ks[sub])]))
     limits = (int(p[:, 0].max()), int(p[:, 1].max()), int(p[:, 2].max()), 100)
-    plan = idx.search_plan(8192, limits, calib=q[:2048])
-    plan2 = idx.search_plan(8192, limits, calib=q[:2048])  # a second plan: two batches in flight
+    plans = [idx.search_plan(8192, limits, calib=q[:2048]) for _ in range(args.in_flight)]
+    plan = plans[0]
     out = np.zeros((8192, 100), np.int32)
     for w in range(3):
-        plan.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
-        plan2.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
+        for pl in plans:
+            pl.run(q[:sizes[w]], p[:sizes[w]], out[:sizes[w]])
     # one batch in flight: submit, wait, next
     lat1, s_ = [], 0
     ids1 = np.zeros((total, 100), np.int32)
@@ -411,10 +411,11 @@ def measure_batching(E, X, args):
         ids1[s_:s_ + b] = out[:b]
         s_ += b
     wall1 = time.perf_counter() - t_all
-    # two batches in flight on two plans (own streams and scratch): batch i is collected just
-    # before batch i + 2 is submitted on the same plan
-    plans, outs = [plan, plan2], [np.zeros((8192, 100), np.int32), np.zeros((8192, 100), np.int32)]
-    pending = [None, None]
+    # F batches in flight on F plans (own streams and scratch): batch i is collected just before
+    # batch i + F is submitted on the same plan
+    F = len(plans)
+    outs = [np.zeros((8192, 100), np.int32) for _ in range(F)]
+    pending = [None] * F
     lat, s_ = [], 0
     ids2 = np.zeros((total, 100), np.int32)
 
@@ -427,14 +428,14 @@ def measure_batching(E, X, args):
 
     t_all = time.perf_counter()
     for i, b in enumerate(sizes):
-        j = i % 2
+        j = i % F
         if pending[j] is not None:
             collect(j)
         ts = time.perf_counter()
         plans[j].submit(q[s_:s_ + b], p[s_:s_ + b])
         pending[j] = (s_, b, ts)
         s_ += b
-    for j in (0, 1):
+    for j in range(F):
         if pending[j] is not None:
             collect(j)
     wall = time.perf_counter() - t_all
@@ -447,16 +448,16 @@ def measure_batching(E, X, args):
            "recall@k": round(recall_all, 4), "extend_scale_per_k": {str(k): v for k, v in chosen.items()},
            "ladder": ladder,
            "plan_threads": plan.threads, "graph": "K=20 (trees 8, ml 8, iter 8, L 40, check 25, S 10)",
-           "graph_build_s": round(build_s, 3), "in_flight": 2,
+           "graph_build_s": round(build_s, 3), "in_flight": F,
            "one_in_flight": {"value": round(total / wall1, 1),
                              "batch_latency_ms": {"p50": round(float(np.percentile(lat1, 50)) * 1e3, 3),
                                                   "p99": round(float(np.percentile(lat1, 99)) * 1e3, 3)}},
            "ids_equal_to_one_in_flight": same,
            "form": "per-query k in {1,10,50,100}, pool = U(6,10) x extend; captured CUDA graphs replayed per "
-                   "batch (host queries in, ids out) on two plans with their own streams, scratch and pinned "
-                   "staging, two batches in flight; persistent kernel, autotuned block size"}
-    plan.close()
-    plan2.close()
+                   "batch (host queries in, ids out) on %d plans with their own streams, scratch and pinned "
+                   "staging, %d batches in flight; persistent kernel, autotuned block size" % (F, F)}
+    for pl in plans:
+        pl.close()
     idx.close()
     return res
 
@@ -772,6 +773,7 @@ def main():
     ap.add_argument("--no-hashing", action="store_true", help="skip the hashing-seeded search")
     ap.add_argument("--no-kgraph", action="store_true", help="skip the kgraph search (method 1)")
     ap.add_argument("--batch-queries", type=int, default=200_000)
+    ap.add_argument("--in-flight", type=int, default=4, help="batches in flight in the batching form")
     ap.add_argument("--train-queries", type=int, default=50_000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -49,6 +49,7 @@ struct efg_hash {
   DevBuf<unsigned long long> binom;    // (HB_MAX_BITS + 1) x (HB_MAX_RADIUS + 1) binomials
   DevBuf<unsigned long long> rstart;   // radius r's first mask index, r = 0..radius+1
   DevBuf<uint32_t> seeds;
+  DevBuf<uint32_t> counts;             // entries of each seed row before its padding
   DevBuf<unsigned long long> qcodes;   // staged query codes (host entry point)
 };
 
@@ -72,7 +73,8 @@ __global__ void __launch_bounds__(256) hash_seed_kernel(const HashSlot* __restri
                                                        const unsigned long long* __restrict__ binom_g,
                                                        const unsigned long long* __restrict__ rstart_g,
                                                        const unsigned long long* __restrict__ qcodes, uint64_t qstride,
-                                                       uint64_t nq, uint32_t cap_q, uint32_t* __restrict__ seeds) {
+                                                       uint64_t nq, uint32_t cap_q, uint32_t* __restrict__ seeds,
+                                                       uint32_t* __restrict__ counts) {
   __shared__ unsigned long long binom[(HB_MAX_BITS + 1) * BR];
   __shared__ unsigned long long rstart[HB_MAX_RADIUS + 2];
   for (uint32_t i = threadIdx.x; i < (HB_MAX_BITS + 1) * BR; i += blockDim.x) binom[i] = binom_g[i];
@@ -144,10 +146,31 @@ __global__ void __launch_bounds__(256) hash_seed_kernel(const HashSlot* __restri
     }
     written += sum;
   }
-  for (uint64_t e = (written < cap_q ? written : cap_q) + lane; e < cap_q; e += 32) row[e] = 0xffffffffu;
+  const uint32_t filled = written < cap_q ? (uint32_t)written : cap_q;
+  if (counts) {  // the search reads only this much of the row
+    if (lane == 0) counts[qi] = filled;
+  } else {
+    for (uint64_t e = filled + lane; e < cap_q; e += 32) row[e] = 0xffffffffu;
+  }
 }
 
 }  // namespace
+
+// Probe sequences of nq queries into rows of cap_q seeds (with counts: the entries present per row,
+// the rest of the row left as it was; without: the rest padded with 0xffffffff).
+int efg::hash_seed_rows(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_stride, uint64_t nq,
+                        uint32_t seeds_per_query, uint32_t* d_seeds, uint32_t* d_counts, cudaStream_t s) {
+  if (nq == 0 || seeds_per_query == 0) return EFG_OK;
+  const uint64_t warps_per_block = 8;
+  const uint64_t blocks = (nq + warps_per_block - 1) / warps_per_block;
+  if (blocks > 0x7fffffffull) return fail(EFG_ERR_ARG, "too many queries for one launch");
+  hash_seed_kernel<<<(unsigned)blocks, 256, 0, s>>>(h->slots.p, h->cap - 1, h->ids.p, h->n, h->tables, h->bits,
+                                                  h->radius, h->binom.p, h->rstart.p,
+                                                  reinterpret_cast<const unsigned long long*>(d_qcodes),
+                                                  qcode_stride, nq, seeds_per_query, d_seeds, d_counts);
+  EFG_CUDA(cudaGetLastError());
+  return EFG_OK;
+}
 
 extern "C" {
 
@@ -245,15 +268,7 @@ int efg_hash_seeds_device(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_
                           uint32_t seeds_per_query, uint32_t* d_seeds, void* stream) {
   if (!h || ((!d_qcodes || !d_seeds) && nq && seeds_per_query)) return fail(EFG_ERR_ARG, "null argument");
   if (qcode_stride < nq) return fail(EFG_ERR_ARG, "qcode_stride < nq");
-  if (nq == 0 || seeds_per_query == 0) return EFG_OK;
-  const uint64_t warps_per_block = 8;
-  const uint64_t blocks = (nq + warps_per_block - 1) / warps_per_block;
-  if (blocks > 0x7fffffffull) return fail(EFG_ERR_ARG, "too many queries for one launch");
-  hash_seed_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
-      h->slots.p, h->cap - 1, h->ids.p, h->n, h->tables, h->bits, h->radius, h->binom.p, h->rstart.p,
-      reinterpret_cast<const unsigned long long*>(d_qcodes), qcode_stride, nq, seeds_per_query, d_seeds);
-  EFG_CUDA(cudaGetLastError());
-  return EFG_OK;
+  return hash_seed_rows(h, d_qcodes, qcode_stride, nq, seeds_per_query, d_seeds, nullptr, (cudaStream_t)stream);
 }
 
 int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64_t nq, uint64_t row_stride,
@@ -266,7 +281,7 @@ int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64
   const SearchParams& sp = idx->sp;
   const bool buckets_only = !idx->graph.valid;  // getNeighbors32 / getNeighbors64 (:929-1085)
   if (!buckets_only && sp.method == 0) {  // the hashing initialiser's kgraph search (its method 0)
-    KgSeedSource src{h, d_qcodes, qcode_stride, h->tables, &h->seeds};
+    KgSeedSource src{h, d_qcodes, qcode_stride, h->tables, &h->seeds, &h->counts};
     return kgraph_search_device(idx, d_q, nq, row_stride, k, d_out, (cudaStream_t)stream, false, &src);
   }
   if (!buckets_only && sp.method != 1) return fail(EFG_ERR_ARG, "no such searching method");
@@ -277,11 +292,12 @@ int efg_hash_search_device(efg_index* idx, efg_hash* h, const float* d_q, uint64
   const uint64_t chunk = std::max<uint64_t>(1, HB_SEED_CHUNK / cap_q);
   cudaStream_t s = (cudaStream_t)stream;
   EFG_TRY(h->seeds.reserve(std::min(chunk, nq) * cap_q));
+  EFG_TRY(h->counts.reserve(std::min(chunk, nq)));
   for (uint64_t q0 = 0; q0 < nq; q0 += chunk) {
     const uint64_t m = std::min(chunk, nq - q0);
-    EFG_TRY(efg_hash_seeds_device(h, d_qcodes + q0, qcode_stride, m, cap_q, h->seeds.p, s));
+    EFG_TRY(hash_seed_rows(h, d_qcodes + q0, qcode_stride, m, cap_q, h->seeds.p, h->counts.p, s));
     EFG_TRY(search_device_ex(idx, d_q + q0 * row_stride, m, row_stride, lim, nullptr, nullptr, d_out + q0 * k, s,
-                             false, h->seeds.p, cap_q, false, buckets_only));
+                             false, h->seeds.p, cap_q, false, buckets_only, h->counts.p));
   }
   return EFG_OK;
 }
@@ -322,6 +338,7 @@ void efg_hash_destroy(efg_hash* h) {
   h->binom.release();
   h->rstart.release();
   h->seeds.release();
+  h->counts.release();
   h->qcodes.release();
   delete h;
 }

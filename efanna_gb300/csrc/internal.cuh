@@ -174,7 +174,7 @@ int search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, u
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
                      bool count_evals, const uint32_t* d_seeds = nullptr, uint32_t seeds_per_query = 0,
-                     bool use_trees = true, bool bucket_only = false);
+                     bool use_trees = true, bool bucket_only = false, const uint32_t* d_seed_counts = nullptr);
 // Builds the BF16 screening copy of the base (round to nearest even, rows padded with zeros).
 int make_base16(efg_index* idx);
 // Builds the FP8 e4m3 screening copy of the base with one FP32 scale per row.
@@ -191,7 +191,12 @@ struct KgSeedSource {
   uint64_t qstride;
   uint32_t tables;
   DevBuf<uint32_t>* buf;  // seed rows, grown as needed
+  DevBuf<uint32_t>* cnt;  // entries present per seed row
 };
+// hashing.cu: the probe sequences of nq queries into seed rows of seeds_per_query entries; with
+// d_counts, the entries present per row (the row's rest untouched), else rows padded with 0xffffffff.
+int hash_seed_rows(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_stride, uint64_t nq,
+                   uint32_t seeds_per_query, uint32_t* d_seeds, uint32_t* d_counts, cudaStream_t s);
 int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, uint32_t k, int32_t* d_out,
                          cudaStream_t s, bool count_evals, const KgSeedSource* hs = nullptr);
 

@@ -345,7 +345,11 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(nq, (512ull << 20) / (init * 8)));
   if (hs) chunk = std::max<uint64_t>(1, std::min<uint64_t>(chunk, (512ull << 20) / (cap * 4)));
   EFG_TRY(idx->kg_keys.reserve(chunk * init));
-  if (hs) EFG_TRY(hs->buf->reserve(chunk * cap));
+  if (hs) {
+    EFG_TRY(hs->buf->reserve(chunk * cap));
+    EFG_TRY(hs->cnt->reserve(chunk));
+    cfg.seed_cnt = hs->cnt->p;
+  }
   EFG_CUDA(cudaFuncSetAttribute(kgraph_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int dev = 0, sms = 152, per_sm = 1;
   cudaGetDevice(&dev);
@@ -372,7 +376,7 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
     uint64_t m = std::min(chunk, nq - q0);
     int l = 0;
     if (hs) {
-      rc = efg_hash_seeds_device(hs->h, hs->d_qcodes + q0, hs->qstride, m, (uint32_t)cap, hs->buf->p, s);
+      rc = hash_seed_rows(hs->h, hs->d_qcodes + q0, hs->qstride, m, (uint32_t)cap, hs->buf->p, hs->cnt->p, s);
       if (rc != EFG_OK) break;
       ++launches;
     }

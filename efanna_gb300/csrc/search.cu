@@ -383,7 +383,7 @@ int finish_search_stats(efg_index* idx, cudaStream_t s, cudaEvent_t e0, cudaEven
 int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld, const efg_query_params& lim_in,
                      const efg_query_params* d_params, const uint32_t* d_nq, int32_t* d_out, cudaStream_t s,
                      bool count_evals, const uint32_t* d_seeds, uint32_t seeds_per_query, bool use_trees,
-                     bool bucket_only) {
+                     bool bucket_only, const uint32_t* d_seed_counts) {
   NvtxRange range("efg: nnexp search");
   const SearchParams& sp = idx->sp;
   efg_query_params lim = lim_in;
@@ -416,6 +416,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
   cfg.seed = idx->bp.seed;
   cfg.nseq = cfg.T * cfg.lsize;
   cfg.nseeds = d_seeds ? seeds_per_query : 0;
+  cfg.seed_cnt = d_seeds ? d_seed_counts : nullptr;
   cfg.fill_k = bucket_only ? 1 : 0;
   if (idx->precision == EFG_PRECISION_FP8) {
     if (!idx->base8.p) EFG_TRY(make_base8(idx));

@@ -30,7 +30,8 @@ struct SearchCfg {
   uint32_t emit_pool;   // stop after the pool and write its keys (kgraph's first stage)
   uint32_t fixed_k;     // graph degree when every row has it (0: row pointers), and
   uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices
-  uint32_t nseeds;      // entry seeds per query placed ahead of the leaves (learned form)
+  uint32_t nseeds;      // entry seeds per query placed ahead of the leaves (the seed rows' stride)
+  const uint32_t* seed_cnt;  // per query, how many of its row's seeds are present (nullptr: all)
   uint32_t fill_k;      // 1: the random fill tops the pool up to k only (the graph-less bucket search)
   uint64_t seed;
 };

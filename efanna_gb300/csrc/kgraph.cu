@@ -361,7 +361,7 @@ int kgraph_search_device(efg_index* idx, const float* d_q, uint64_t nq, uint64_t
   uint64_t grid = std::max<uint64_t>(1, warps / KG_WARPS);
   EFG_TRY(idx->kg_bits.reserve(grid * KG_WARPS * kc.words));
 
-  EFG_TRY(idx->eval_counter.reserve(4));
+  EFG_TRY(idx->eval_counter.reserve(8));
   EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 32, s));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

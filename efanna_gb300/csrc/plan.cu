@@ -122,7 +122,7 @@ int plan_build(efg_search_plan* p, const float* calib_queries, uint64_t n_calib)
   EFG_TRY(p->params.reserve(capacity));
   EFG_TRY(p->out.reserve(capacity * (uint64_t)p->lim.k));
   EFG_TRY(p->nq.reserve(1));
-  EFG_TRY(p->eval_counter.reserve(4));
+  EFG_TRY(p->eval_counter.reserve(8));
   if (cudaMallocHost((void**)&p->hq, capacity * idx->ld * sizeof(float)) != cudaSuccess ||
       cudaMallocHost((void**)&p->hparams, capacity * sizeof(efg_query_params)) != cudaSuccess ||
       cudaMallocHost((void**)&p->hout, capacity * (uint64_t)p->lim.k * sizeof(int32_t)) != cudaSuccess ||

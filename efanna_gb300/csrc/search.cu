@@ -326,6 +326,12 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
     EFG_TRY(idx->ovf_list.reserve(nq + 1));
     EFG_CUDA(cudaMemsetAsync(idx->ovf_list.p, 0, 4, s));
   }
+  // the two passes' query counters, after the four statistics words
+  EFG_TRY(idx->eval_counter.reserve(8));
+  uint32_t* qctr = reinterpret_cast<uint32_t*>(idx->eval_counter.p + 4);
+  EFG_CUDA(cudaMemsetAsync(qctr, 0, 2 * sizeof(uint32_t), s));
+  c1.next_q = qctr;
+  c2.next_q = qctr + 1;
   const Forest& F = idx->forest;
   kernel<<<(unsigned)grid1, threads, smem1, s>>>(
       idx->d_base, idx->n, idx->dim, idx->ld, F.nodes.p, F.nleaf.p, F.cnl.p, F.d_roots.p, F.leaves.p, idx->graph.ptr.p,
@@ -438,7 +444,7 @@ int search_device_ex(efg_index* idx, const float* d_q, uint64_t nq, uint64_t qld
     if (k > cfg.rerank) return fail(EFG_ERR_ARG, "k above 1024 is not supported with BF16 screening");
   }
   uint32_t maxdeg = graph_max_degree(idx);
-  EFG_TRY(idx->eval_counter.reserve(4));
+  EFG_TRY(idx->eval_counter.reserve(8));
   EFG_CUDA(cudaMemsetAsync(idx->eval_counter.p, 0, 32, s));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

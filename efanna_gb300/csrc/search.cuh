@@ -32,6 +32,7 @@ struct SearchCfg {
   uint32_t kmagic;      // ceil(2^32 / fixed_k) for the division of item indices
   uint32_t nseeds;      // entry seeds per query placed ahead of the leaves (the seed rows' stride)
   const uint32_t* seed_cnt;  // per query, how many of its row's seeds are present (nullptr: all)
+  uint32_t* next_q;          // the launch's query counter: CTAs take queries as they come free
   uint32_t fill_k;      // 1: the random fill tops the pool up to k only (the graph-less bucket search)
   uint64_t seed;
 };

@@ -618,12 +618,15 @@ __global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, const uin
                              const uint64_t* __restrict__ rec_off, const uint64_t* __restrict__ rec_key,
                              const uint32_t* __restrict__ rec_aux, float* __restrict__ pd,
                              uint32_t* __restrict__ pid, uint32_t* __restrict__ Lc, float* __restrict__ radius,
-                             uint8_t* __restrict__ found) {
-  uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint32_t lane = threadIdx.x & 31;
+                             uint8_t* __restrict__ found, uint32_t* __restrict__ next_node) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (;;) {  // nodes taken from a shared counter as warps come free (their record counts differ)
+  uint32_t tt = 0;
+  if (lane == 0) tt = atomicAdd(next_node, 1u);
+  const uint64_t t = __shfl_sync(0xffffffffu, tt, 0);
   if (t >= n) return;
   uint32_t B = cnt[t];
-  if (B == 0) return;
+  if (B == 0) continue;
   const uint64_t* rk = rec_key + rec_off[t];
   const uint32_t* ra = rec_aux + rec_off[t];
   WarpPool<NS> pool;
@@ -733,6 +736,7 @@ __global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, const uin
   if (lane == 0) {
     Lc[t] = L;
     radius[t] = rad;
+  }
   }
 }
 
@@ -1015,9 +1019,9 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.found.p, 0, n, s));
-  LocalBuf<uint32_t> jctr;  // the two passes' node counters
-  EFG_TRY(jctr.reserve(2));
-  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 8, s));
+  LocalBuf<uint32_t> jctr;  // node counters of the two join passes and the merge
+  EFG_TRY(jctr.reserve(3));
+  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 12, s));
   int sms = 152, per0 = 1, per1 = 1, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1040,22 +1044,19 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
                                              S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.rec_off64.p,
                                              S.cursor.p, S.rec_key.p, S.rec_aux.p, jctr.p + 1);
   EFG_CUDA(cudaGetLastError());
+  const unsigned mgrid = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * 8);
   if (S.P <= 32)
-    merge_kernel<1><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,
-                                                            S.rec_aux.p, S.pd.p, S.pid.p, S.Lc.p, S.radius.p,
-                                                            S.found.p);
+    merge_kernel<1><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else if (S.P <= 64)
-    merge_kernel<2><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,
-                                                            S.rec_aux.p, S.pd.p, S.pid.p, S.Lc.p, S.radius.p,
-                                                            S.found.p);
+    merge_kernel<2><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else if (S.P <= 128)
-    merge_kernel<4><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,
-                                                            S.rec_aux.p, S.pd.p, S.pid.p, S.Lc.p, S.radius.p,
-                                                            S.found.p);
+    merge_kernel<4><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else
-    merge_kernel<8><<<blocks_for(n * 32, 256), 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p,
-                                                            S.rec_aux.p, S.pd.p, S.pid.p, S.Lc.p, S.radius.p,
-                                                            S.found.p);
+    merge_kernel<8><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   EFG_CUDA(cudaGetLastError());
   // ---- update
   update_range_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, S.P, bp.S, S.pd.p, S.pid.p, S.Lc.p, S.Range.p,

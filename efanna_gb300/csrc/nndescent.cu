@@ -146,7 +146,6 @@ __global__ void __launch_bounds__(256, 3) merge_route_kernel(const float* __rest
   for (uint64_t wb = gwarp * 32; wb < ntasks; wb += nwarps * 32) {
     const uint64_t myw = wb + lane;
     uint32_t myp = 0, mls = 0, mle = 0;
-    int32_t mleaf = 0;
     uint64_t mt = 0;
     if (myw < ntasks) {
       // node owning task myw: last v with task_off[v] <= myw
@@ -169,7 +168,6 @@ __global__ void __launch_bounds__(256, 3) merge_route_kernel(const float* __rest
         cur = x < nd.div_val ? nd.left : nd.right;
         nd = tv.nodes[cur];
       }
-      mleaf = cur;
       mls = (uint32_t)(-(nd.left + 1));
       mle = (uint32_t)nd.right;
       if (PASS == 0 && task_d) {
@@ -229,7 +227,6 @@ __global__ void __launch_bounds__(256, 3) merge_route_kernel(const float* __rest
         }
       }
     }
-    (void)mleaf;
   }
   if (PASS == 0 && lane == 0 && local) atomicAdd(ndist, local);
 }

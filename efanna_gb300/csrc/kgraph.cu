@@ -81,38 +81,72 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, uint32_t lane) {
   return v;
 }
 
+// Sums v[0..4) over the warp's 32 lanes; lane l returns the total of v[(l >> 3) & 3].
+__device__ __forceinline__ float reduce4_rows(const float* v, uint32_t lane) {
+  const bool b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1;
+  float h[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    float keep = b4 ? v[j + 2] : v[j], send = b4 ? v[j] : v[j + 2];
+    h[j] = keep + __shfl_xor_sync(FULL, send, 16);
+  }
+  float keep = b3 ? h[1] : h[0], send = b3 ? h[0] : h[1];
+  float x = keep + __shfl_xor_sync(FULL, send, 8);
+  x += __shfl_xor_sync(FULL, x, 4);
+  x += __shfl_xor_sync(FULL, x, 2);
+  x += __shfl_xor_sync(FULL, x, 1);
+  return x;
+}
+
+// U rows (8 or 4) of the query's distances: rows u0 .. u0+U-1 of the lanes' ids (the last one
+// repeated past cnt); lane u0 + u receives row u's distance in `mine`.
+template <int U>
+__device__ __forceinline__ void row_dists_pass(const float4* qv, uint32_t ld4, const float* __restrict__ base,
+                                               uint32_t ld, uint32_t id, uint32_t cnt, uint32_t u0, uint32_t lane,
+                                               float& mine) {
+  uint32_t rid[U];
+  float acc[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    rid[u] = __shfl_sync(FULL, id, u0 + u < cnt ? u0 + u : u0);
+    acc[u] = 0.f;
+  }
+  for (uint32_t c = lane; c < ld4; c += 32) {
+    float4 qc = qv[c];
+    float4 x[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) x[u] = __ldg(reinterpret_cast<const float4*>(base + (uint64_t)rid[u] * ld) + c);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float d0 = x[u].x - qc.x, d1 = x[u].y - qc.y, d2 = x[u].z - qc.z, d3 = x[u].w - qc.w;
+      acc[u] += d0 * d0;
+      acc[u] += d1 * d1;
+      acc[u] += d2 * d2;
+      acc[u] += d3 * d3;
+    }
+  }
+  // the U sums reduced together (U = 8: lanes 4r .. 4r+3 end with row r's; U = 4: lanes 8r .. 8r+7),
+  // then row u's sum moves to lane u0 + u
+  if (U == 8) {
+    const float tot = reduce8_rows(acc, lane);
+    const float t = __shfl_sync(FULL, tot, ((lane - u0) & 7) * 4);
+    if (lane - u0 < 8u) mine = t;
+  } else {
+    const float tot = reduce4_rows(acc, lane);
+    const float t = __shfl_sync(FULL, tot, ((lane - u0) & 3) * 8);
+    if (lane - u0 < 4u) mine = t;
+  }
+}
+
 // Squared distances from the query (shared memory, ld4 float4, zero padded) to the rows named by
-// lanes 0..cnt-1 (`id`); lane u returns row u's distance.  Eight rows are in flight per pass.
+// lanes 0..cnt-1 (`id`); lane u returns row u's distance.  Eight rows are in flight per pass, four
+// in a last pass of at most four rows (most expansions bring fewer than five new neighbours).
 __device__ __forceinline__ float warp_row_dists(const float4* qv, uint32_t ld4, const float* __restrict__ base, uint32_t ld,
                                 uint32_t id, uint32_t cnt, uint32_t lane) {
   float mine = 0.f;
   for (uint32_t u0 = 0; u0 < cnt; u0 += 8) {
-    uint32_t rid[8];
-    float acc[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      rid[u] = __shfl_sync(FULL, id, u0 + u < cnt ? u0 + u : u0);
-      acc[u] = 0.f;
-    }
-    for (uint32_t c = lane; c < ld4; c += 32) {
-      float4 qc = qv[c];
-      float4 x[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) x[u] = __ldg(reinterpret_cast<const float4*>(base + (uint64_t)rid[u] * ld) + c);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        float d0 = x[u].x - qc.x, d1 = x[u].y - qc.y, d2 = x[u].z - qc.z, d3 = x[u].w - qc.w;
-        acc[u] += d0 * d0;
-        acc[u] += d1 * d1;
-        acc[u] += d2 * d2;
-        acc[u] += d3 * d3;
-      }
-    }
-    // the eight sums reduced together (lanes 4r .. 4r+3 end with row r's), then row u's sum
-    // moves to lane u0 + u
-    const float tot = reduce8_rows(acc, lane);
-    const float t = __shfl_sync(FULL, tot, ((lane - u0) & 7) * 4);
-    if (lane - u0 < 8u) mine = t;
+    if (cnt - u0 <= 4) row_dists_pass<4>(qv, ld4, base, ld, id, cnt, u0, lane, mine);
+    else row_dists_pass<8>(qv, ld4, base, ld, id, cnt, u0, lane, mine);
   }
   return mine;
 }

@@ -583,7 +583,7 @@ def measure_kgraph(E, idx, Q, gt, nq, stream, ws, args):
 
 # the hashing-seeded search: 8 tables of 20-bit sign-of-projection codes, Hamming radius 2
 HASH_TABLES, HASH_BITS, HASH_RADIUS = 8, 20, 2
-HASH_LADDER = [(4, 4000, 750), (4, 5000, 800), (4, 6000, 800), (6, 8000, 1000)]
+HASH_LADDER = [(4, 4000, 750), (4, 4500, 800), (4, 5000, 800), (4, 6000, 800), (6, 8000, 1000)]
 
 
 def measure_hashing(E, idx, x, q, Q, gt, nq, stream, ws, args):

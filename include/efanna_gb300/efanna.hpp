@@ -32,6 +32,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 #include <algorithm>
@@ -296,6 +297,9 @@ class FIndex {
   void setSearchParams(int epochs, int init_num, int extend_to, int search_trees = 0, int search_lv = -1,
                        int search_method = 0) {
     method_ = search_method;
+    sp_epochs_ = epochs;
+    sp_init_ = init_num;
+    sp_extend_ = extend_to > init_num ? init_num : extend_to;
     check(efg_set_search_params(idx_, epochs, init_num, extend_to, search_trees, search_lv, search_method));
   }
   size_t getGraphSize() { return (size_t)efg_graph_size(idx_); }
@@ -308,7 +312,74 @@ class FIndex {
     }
     return row;
   }
-  void outputVisitBucketNum() {}
+  // The hashing index's histogram of the last search (hashing_index.hpp:1618-1626, counted at
+  // :1133-1143): per radius, the masks it holds and the queries whose pool filled within it
+  // (a pool that filled at the first mask of the next radius counts for the smaller one, as in
+  // the reference), then the queries whose pool the Hamming ball could not fill.  Recomputed here
+  // on the host from the codes; the KD-tree index prints nothing, as in the reference.
+  void outputVisitBucketNum() {
+    if (!hashing_ || !last_nq_) return;
+    if (vb_maps_.empty()) {
+      const size_t n = base_codes_.size() / (size_t)tables_;
+      vb_maps_.resize((size_t)tables_);
+      for (int h = 0; h < tables_; ++h)
+        for (size_t i = 0; i < n; ++i) vb_maps_[(size_t)h][base_codes_[(size_t)h * n + i]].push_back((uint32_t)i);
+    }
+    const size_t n = base_codes_.size() / (size_t)tables_;
+    std::vector<uint64_t> masks(1, 0);
+    std::vector<uint64_t> radius_end(1, 1);  // HammingRadius
+    std::vector<int> pos;
+    for (int r = 1; r <= radius_; ++r) {
+      pos.assign((size_t)r, 0);
+      for (int t = 0; t < r; ++t) pos[(size_t)t] = t;
+      for (;;) {
+        uint64_t m = 0;
+        for (int t = 0; t < r; ++t) m |= 1ull << pos[(size_t)t];
+        masks.push_back(m);
+        int t = r - 1;
+        while (t >= 0 && pos[(size_t)t] == bits_ - r + t) --t;
+        if (t < 0) break;
+        ++pos[(size_t)t];
+        for (int u = t + 1; u < r; ++u) pos[(size_t)u] = pos[(size_t)u - 1] + 1;
+      }
+      radius_end.push_back(masks.size());
+    }
+    std::vector<unsigned> visit((size_t)radius_ + 2, 0);
+    std::vector<uint32_t> stamp(n, 0);
+    const size_t nq = last_nq_;
+    for (size_t q = 0; q < nq; ++q) {
+      unsigned p = 0;
+      size_t j = 0;
+      for (; j < masks.size(); ++j) {
+        for (int h = 0; h < tables_ && p < last_pool_; ++h) {
+          auto it = vb_maps_[(size_t)h].find(query_codes_[(size_t)h * nq + q] ^ masks[j]);
+          if (it == vb_maps_[(size_t)h].end()) continue;
+          for (size_t e = 0; e < it->second.size() && p < last_pool_; ++e) {
+            uint32_t id = it->second[e];
+            if (stamp[id] == (uint32_t)q + 1) continue;
+            stamp[id] = (uint32_t)q + 1;
+            ++p;
+          }
+        }
+        if (p >= last_pool_) break;
+      }
+      if (p < last_pool_) {
+        ++visit[(size_t)radius_ + 1];
+      } else {
+        for (int r = 0; r <= radius_; ++r)
+          if (j <= radius_end[(size_t)r]) {
+            ++visit[(size_t)r];
+            break;
+          }
+      }
+    }
+    std::cout << "Radius 0 bucket num: " << radius_end[0] << " points num: " << visit[0] << std::endl;
+    size_t i = 1;
+    for (; i < radius_end.size(); ++i)
+      std::cout << "Radius " << i << " bucket num: " << radius_end[i] - radius_end[i - 1]
+                << " points num: " << visit[i] << std::endl;
+    std::cout << "Radius larger, points num: " << visit[i] << std::endl;
+  }
 
  private:
   static void check(int rc) {
@@ -400,8 +471,17 @@ class FIndex {
     if (query_codes_.size() != nq * (size_t)tables_)
       throw std::runtime_error("the query code files hold a different number of queries");
     std::vector<int32_t> out(nq * (size_t)k);
+    // the pool size this search fills (the kgraph search raises the stored size to epochs *
+    // extend_to first, as the reference does) -- kept for outputVisitBucketNum
+    unsigned pool = (unsigned)sp_init_;
+    if (efg_graph_size(idx_) != 0 && method_ == 0 && (unsigned)(sp_epochs_ * sp_extend_) >= pool) {
+      pool = (unsigned)(sp_epochs_ * sp_extend_);
+      sp_init_ = (int)pool;
+    }
     check(efg_hash_search(idx_, hash_, reinterpret_cast<const float*>(query.data()), nq, (uint32_t)query.get_cols(),
                           query.get_stride(), query_codes_.data(), (uint32_t)k, out.data()));
+    last_nq_ = nq;
+    last_pool_ = pool;
   }
 
   IndexParams index_params_;
@@ -410,7 +490,11 @@ class FIndex {
   efg_hash* hash_ = nullptr;
   bool hashing_ = false;
   int method_ = 0, tables_ = 0, bits_ = 0, radius_ = 0;
+  int sp_epochs_ = 0, sp_init_ = 0, sp_extend_ = 0;
+  size_t last_nq_ = 0;
+  unsigned last_pool_ = 0;
   std::vector<uint64_t> base_codes_, query_codes_;
+  std::vector<std::unordered_map<uint64_t, std::vector<uint32_t> > > vb_maps_;
 };
 
 }  // namespace efanna

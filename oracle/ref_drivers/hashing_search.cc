@@ -70,5 +70,6 @@ int main(int argc, char** argv) {
                         argc == 17 ? std::atoi(argv[16]) : 1);
   index.knnSearch(std::atoi(argv[15]), queries);
   index.saveResults(argv[6]);
+  index.outputVisitBucketNum();  // the per-radius histogram of the search (stdout)
   return 0;
 }

@@ -21,7 +21,8 @@ across runs) on small seeded integer-valued data, and stores inputs and outputs:
                files, for each parameter set in HASH_POINTS: the codes as read back (tables x n and
                tables x nq, after the shift), the code length in effect and the ids; the same for
                its kgraph search (search method 0 there) as kgraph_<i> and for its search without
-               a graph (the bucket search) as buckets_<i>.
+               a graph (the bucket search) as buckets_<i>; the lines outputVisitBucketNum printed
+               after each search as visit_<i>, visit_kgraph_<i>, visit_buckets_<i>.
 
 ``--only-kgraph`` / ``--only-hashing`` regenerate just those fixtures.
 
@@ -120,11 +121,14 @@ def make_hashing(name, tmp):
         io.write_codes(qpre, datasets.sign_codes(q, tables, clen, seed=100 + i, center=x.mean(0)), clen)
         args = [O.ref_bin("hashing_search", "strict"), base, os.path.join(HERE, name + ".graph"), qf, bpre, qpre, r,
                 str(clen), str(tables), str(up), str(rad), str(shift), str(ep), str(pool), str(ext), str(k)]
-        run(args + ["0"], 1)
+        def radius_lines(text):
+            return np.array([ln for ln in text.splitlines() if ln.startswith("Radius")])
+
+        out["visit_kgraph_%d" % i] = radius_lines(run(args + ["0"], 1))
         out["kgraph_%d" % i] = io.read_ivecs(r)
-        run(args[:2] + ["-"] + args[3:], 1)
+        out["visit_buckets_%d" % i] = radius_lines(run(args[:2] + ["-"] + args[3:], 1))
         out["buckets_%d" % i] = io.read_ivecs(r)
-        run(args, 1)
+        out["visit_%d" % i] = radius_lines(run(args, 1))
         bc, bits = io.read_codes(bpre, tables, clen, shift)
         qc, _ = io.read_codes(qpre, tables, clen, shift)
         word = np.uint32 if bits <= 32 else np.uint64

@@ -197,3 +197,7 @@ def test_reference_api_program_through_facade(efg, oracle_lib, case, tmp_path):
             ref, _, _ = O.search_hashed_kgraph(x, gp, gi, q, bc, qc, bits, rad, k=k, epochs=ep, init_num=pool,
                                                extend_to=ext, mode=O.CANON, threads=4)
         assert np.array_equal(io.read_ivecs(rf), ref), (i, method)
+        # outputVisitBucketNum after the search prints the reference's histogram lines
+        key = {1: "visit_%d", 0: "visit_kgraph_%d", -1: "visit_buckets_%d"}[method] % i
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("Radius")]
+        assert lines == [str(v) for v in hz[key]], (i, method, lines)

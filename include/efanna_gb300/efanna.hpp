@@ -284,11 +284,22 @@ class FIndex {
     }
     check(rc);
   }
-  void saveIndex(char* filename) { file(efg_save_index(idx_, filename), -10086); }
-  void loadIndex(char* filename) { file(efg_load_index(idx_, filename), -10087); }
-  void saveTrees(char* filename) { file(efg_save_trees(idx_, filename), -10086); }
-  void loadTrees(char* filename) { file(efg_load_trees(idx_, filename), -10087); }
+  // the hashing index's index, trees and graph writers and index/trees loaders do nothing in the
+  // reference (hashing_index.hpp:1628-1655); only its loadGraph reads a file
+  void saveIndex(char* filename) {
+    if (!hashing_) file(efg_save_index(idx_, filename), -10086);
+  }
+  void loadIndex(char* filename) {
+    if (!hashing_) file(efg_load_index(idx_, filename), -10087);
+  }
+  void saveTrees(char* filename) {
+    if (!hashing_) file(efg_save_trees(idx_, filename), -10086);
+  }
+  void loadTrees(char* filename) {
+    if (!hashing_) file(efg_load_trees(idx_, filename), -10087);
+  }
   void saveGraph(char* filename) {
+    if (hashing_) return;
     int rc = efg_save_graph(idx_, filename);
     if (rc != EFG_ERR_STATE) file(rc, -10086);  // no graph: the reference writes an empty file
   }

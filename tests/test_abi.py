@@ -46,3 +46,43 @@ def test_argument_errors_without_gpu(efg):
     assert rc == efg.EFG_ERR_ARG  # fewer than 2*S+2 points
     rc = efg.lib().efg_index_create(None, 4, 8, 8, C.byref(p), C.byref(h))
     assert rc == efg.EFG_ERR_ARG
+
+
+def _declarations():
+    """(return type, name, argument count) of every function the header declares."""
+    txt = open(HEADER).read()
+    out = []
+    for ret, name, args in re.findall(r"^(int|void|uint64_t|uint32_t|const char\*)\s+(efg_[a-z0-9_]+)\s*\(([^)]*)\)",
+                                      txt, re.M):
+        out.append((ret, name, 0 if args.strip() in ("", "void") else args.count(",") + 1))
+    return out
+
+
+def test_every_entry_point_refuses_null_arguments(efg):
+    """Each status-returning entry point called with every argument zero (null handles, null
+    pointers, zero sizes) returns EFG_ERR_ARG with a message, before any GPU work; the getters
+    return 0 and the destroy/default functions accept null.  Runs here, with no GPU."""
+    import ctypes as C
+    lib = C.CDLL(efg.LIB_PATH)  # no argtypes: 64-bit zeros fill pointer and integer slots alike
+    lib.efg_last_error.restype = C.c_char_p
+    decls = _declarations()
+    assert len(decls) >= 50
+    for ret, name, nargs in decls:
+        f = getattr(lib, name)
+        zeros = [C.c_uint64(0)] * nargs
+        if name in ("efg_last_error", "efg_version"):
+            continue
+        if ret == "int":
+            f.restype = C.c_int
+            rc = f(*zeros)
+            if name == "efg_search_plan_threads":  # a thread count, 0 for no plan
+                assert rc == 0
+                continue
+            assert rc == efg.EFG_ERR_ARG, (name, rc)
+            assert lib.efg_last_error(), name
+        elif ret in ("uint64_t", "uint32_t"):
+            f.restype = C.c_uint64 if ret == "uint64_t" else C.c_uint32
+            assert f(*zeros) == 0, name
+        else:
+            f.restype = None
+            f(*zeros)

@@ -54,7 +54,7 @@ def build(verbose: bool = False) -> str:
         objs = list(ex.map(_compile, SOURCES))
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

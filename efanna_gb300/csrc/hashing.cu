@@ -19,6 +19,9 @@
 //     without a graph, the same kernel with no epochs ranks the bucket ids, the random fill topping
 //     the pool up to k only (the graph-less search getNeighbors32 / getNeighbors64, :929-1085).
 #include <algorithm>
+#include <atomic>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -172,6 +175,27 @@ int efg::hash_seed_rows(efg_hash* h, const uint64_t* d_qcodes, uint64_t qcode_st
   return EFG_OK;
 }
 
+// Runs fn(h) for every table h on up to `tables` host threads (the calling one included); the
+// tables are independent, so the result does not depend on the number of threads.
+template <class F>
+static void for_each_table(uint32_t tables, const F& fn) {
+  std::atomic<uint32_t> next{0};
+  auto worker = [&] {
+    for (uint32_t h; (h = next.fetch_add(1)) < tables;) fn(h);
+  };
+  const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+  std::vector<std::thread> pool;
+  for (uint32_t t = 1; t < std::min(tables, hw); ++t) {
+    try {
+      pool.emplace_back(worker);
+    } catch (const std::system_error&) {
+      break;  // fewer threads: the calling thread takes what is left
+    }
+  }
+  worker();
+  for (auto& th : pool) th.join();
+}
+
 extern "C" {
 
 int efg_hash_create(efg_index* idx, const uint64_t* codes, uint32_t tables, uint32_t code_bits, uint32_t radius,
@@ -195,28 +219,36 @@ int efg_hash_create(efg_index* idx, const uint64_t* codes, uint32_t tables, uint
   for (uint32_t r = 0; r <= radius; ++r) rstart[r + 1] = rstart[r] + binom[code_bits * BR + r];
   if (rstart[radius + 1] * tables > HB_MAX_PROBES)
     return fail(EFG_ERR_ARG, "Hamming ball too large: masks * tables must be <= 2^26");
-  // per table: ids sorted by (code, id), unique codes into an open-addressing table at most half full
+  // per table: ids sorted by (code, id), unique codes into an open-addressing table at most half
+  // full; the tables are built on parallel host threads (allocations stay on the calling thread)
   std::vector<std::vector<std::pair<uint64_t, uint32_t>>> sorted(tables);
-  uint64_t maxu = 1;
-  for (uint32_t h = 0; h < tables; ++h) {
+  for (auto& v : sorted) v.resize(n);
+  std::vector<uint64_t> uniq(tables, 0);
+  std::atomic<bool> bad_code{false};
+  for_each_table(tables, [&](uint32_t h) {
     auto& v = sorted[h];
-    v.resize(n);
     for (uint64_t i = 0; i < n; ++i) {
       uint64_t c = codes[(uint64_t)h * n + i];
-      if (c & ~vmask) return fail(EFG_ERR_ARG, "a code has bits above code_bits");
+      if (c & ~vmask) {
+        bad_code = true;
+        return;
+      }
       v[i] = {c, (uint32_t)i};
     }
     std::sort(v.begin(), v.end());
     uint64_t u = 0;
     for (uint64_t i = 0; i < n; ++i) u += i == 0 || v[i].first != v[i - 1].first;
-    maxu = std::max(maxu, u);
-  }
+    uniq[h] = u;
+  });
+  if (bad_code) return fail(EFG_ERR_ARG, "a code has bits above code_bits");
+  uint64_t maxu = 1;
+  for (uint64_t u : uniq) maxu = std::max(maxu, u);
   uint64_t cap = 16;
   while (cap < 2 * maxu) cap *= 2;
   if (cap > (1ull << 31)) return fail(EFG_ERR_ARG, "too many distinct codes");
   std::vector<HashSlot> hslots(cap * tables, HashSlot{0, 0, 0});
   std::vector<uint32_t> hids(n * tables);
-  for (uint32_t h = 0; h < tables; ++h) {
+  for_each_table(tables, [&](uint32_t h) {
     const auto& v = sorted[h];
     HashSlot* tab = hslots.data() + (uint64_t)h * cap;
     for (uint64_t i = 0; i < n;) {
@@ -230,7 +262,7 @@ int efg_hash_create(efg_index* idx, const uint64_t* codes, uint32_t tables, uint
       tab[s] = HashSlot{(unsigned long long)v[i].first, (uint32_t)i, (uint32_t)(e - i)};
       i = e;
     }
-  }
+  });
   efg_hash* H = new efg_hash();
   H->idx = idx;
   H->tables = tables;

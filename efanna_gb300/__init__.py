@@ -21,7 +21,8 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libefanna_gb300.so")
+# EFG_LIBRARY selects another build of the library (the diagnostic phase-clock build)
+LIB_PATH = os.environ.get("EFG_LIBRARY") or os.path.join(HERE, "libefanna_gb300.so")
 
 EFG_OK, EFG_ERR_ARG, EFG_ERR_CUDA, EFG_ERR_MERGE_LEVEL, EFG_ERR_OPEN, EFG_ERR_FORMAT = 0, 1, 2, 3, 4, 5
 EFG_ERR_STATE, EFG_ERR_TREE_COUNT, EFG_ERR_NOMEM, EFG_ERR_DEVICE_LIMIT = 6, 7, 8, 9
@@ -132,7 +133,7 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
+    if not os.path.exists(LIB_PATH) and LIB_PATH == os.path.join(HERE, "libefanna_gb300.so"):
         from . import build as _b
         _b.build()
     L = C.CDLL(LIB_PATH)

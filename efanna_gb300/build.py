@@ -16,6 +16,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libefanna_gb300.so")
+# diagnostic build with per-phase cycle counters in the search kernel (EFG_PHASE_CLOCKS): its own
+# objects and library name, so it never replaces the library above
+PHASE_OUT_DIR = os.path.join(HERE, "_build_phase")
+PHASE_LIB = os.path.join(HERE, "libefanna_gb300_phase.so")
 CLI_SRC = os.path.join(HERE, "cli", "efg_cli.cc")
 CLI = os.path.join(HERE, "cli", "efg_cli")
 SOURCES = ["index.cu", "distance.cu", "search.cu", "kgraph.cu", "plan.cu", "learned.cu", "hashing.cu", "trees.cu", "nndescent.cu", "noalloc.cu"]
@@ -29,38 +33,41 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _flags():
+def _flags(phase_clocks: bool = False):
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
-                   "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "--expt-relaxed-constexpr"]
+                   "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "--expt-relaxed-constexpr"] + \
+        (["-DEFG_PHASE_CLOCKS=1"] if phase_clocks else [])
 
 
-def _compile(src: str) -> str:
-    obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, phase_clocks: bool = False) -> str:
+    obj = os.path.join(PHASE_OUT_DIR if phase_clocks else OUT_DIR, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".inc"))]
     deps.append(os.path.join(ROOT, "include", "efanna_gb300.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [nvcc(), "-c", path, "-o", obj] + _flags()
+    cmd = [nvcc(), "-c", path, "-o", obj] + _flags(phase_clocks)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
     return obj
 
 
-def build(verbose: bool = False) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(verbose: bool = False, phase_clocks: bool = False) -> str:
+    """Builds the library; ``phase_clocks`` builds the diagnostic one (PHASE_LIB) instead."""
+    out_dir, lib = (PHASE_OUT_DIR, PHASE_LIB) if phase_clocks else (OUT_DIR, LIB)
+    os.makedirs(out_dir, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
-    if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-lcudart", "-lpthread"]
+        objs = list(ex.map(lambda src: _compile(src, phase_clocks), SOURCES))
+    if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(o) for o in objs):
+        return lib
+    cmd = [nvcc(), "-shared", "-o", lib] + objs + ARCH + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 def build_cli() -> str:

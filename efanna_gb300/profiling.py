@@ -3,16 +3,20 @@
     python -m efanna_gb300.profiling table <ncu.csv>        per-kernel launch counts, time, share
     python -m efanna_gb300.profiling search [--n N] [--nq Q] [--point E P X] [--trees T]
                                             [--precision fp32|bf16|fp8 ...] [--repeat R]
-                                            [--method 0|1] [--recall]
+                                            [--method 0|1] [--recall] [--phase-clocks]
         builds a graph on the seeded mixture and runs batched searches (R per precision and
         point): the small case used for Nsight Compute captures of nnexp_kernel (N=400k keeps
-        the base above the L2 size).
+        the base above the L2 size).  --phase-clocks runs the same searches on the diagnostic
+        build of the library (EFG_PHASE_CLOCKS: every CTA of nnexp_kernel reports the SM cycles
+        of each phase) and prints each search's phase shares after its line.
 """
 from __future__ import annotations
 
 import argparse
 import collections
 import csv
+import os
+import subprocess
 import sys
 
 import numpy as np
@@ -88,6 +92,49 @@ def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp3
                        s.expanded_nodes / nq, s.overflow_queries, wall, rec))
 
 
+PHASES = ("setup", "tree descent", "leaf-sequence scan", "pool fill", "pool distances", "pool folds",
+          "expansion", "epoch distances", "epoch folds", "output", "rest")
+
+
+def phase_summary(lines) -> str:
+    """Sums the diagnostic build's per-CTA lines ("EFG_PHASE threads queries c0 .. c10") into
+    per-phase shares and cycles per query."""
+    tot = np.zeros(len(PHASES))
+    queries = 0
+    for ln in lines:
+        f = ln.split()
+        queries += int(f[2])
+        tot += np.array([float(v) for v in f[3:3 + len(PHASES)]])
+    if queries == 0 or tot.sum() == 0:
+        return "  (no phase counters)"
+    out = ["  %d CTAs, %d queries, %.0f CTA cycles per query" % (len(lines), queries, tot.sum() / queries)]
+    for name, c in zip(PHASES, tot):
+        out.append("  %-20s %6.1f%%  %9.1f kcycles/query" % (name, 100 * c / tot.sum(), c / queries / 1e3))
+    return "\n".join(out)
+
+
+def run_phase_clocks(argv) -> int:
+    """Builds the diagnostic library, reruns this search command on it and summarises the phase
+    counters printed before each search's line."""
+    from . import build as _b
+    lib = _b.build(phase_clocks=True)
+    env = dict(os.environ, EFG_LIBRARY=lib)
+    args = [a for a in argv if a != "--phase-clocks"]
+    r = subprocess.run([sys.executable, "-m", "efanna_gb300.profiling"] + args, env=env, capture_output=True,
+                       text=True)
+    pending = []
+    for ln in r.stdout.splitlines():
+        if ln.startswith("EFG_PHASE "):
+            pending.append(ln)
+        else:
+            print(ln)
+            if ln.startswith("search "):
+                print(phase_summary(pending))
+                pending = []
+    sys.stderr.write(r.stderr)
+    return r.returncode
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd")
@@ -104,9 +151,13 @@ if __name__ == "__main__":
     s.add_argument("--repeat", type=int, default=2)
     s.add_argument("--method", type=int, default=0, help="0 nnexp, 1 kgraph")
     s.add_argument("--recall", action="store_true", help="also report recall@10 against the exact 10-NN")
+    s.add_argument("--phase-clocks", action="store_true",
+                   help="run on the diagnostic build and print per-phase cycle shares of nnexp_kernel")
     a = ap.parse_args()
     if a.cmd == "table":
         print(launch_table(a.csv))
+    elif a.cmd == "search" and a.phase_clocks:
+        sys.exit(run_phase_clocks(sys.argv[1:]))
     elif a.cmd == "search":
         search_case(a.n, a.nq, a.point, a.trees, a.also, a.precision, a.repeat, a.method, a.recall)
     else:

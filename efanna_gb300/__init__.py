@@ -241,6 +241,12 @@ class Index:
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
+            # the plans, learned models and hash tables of this index use it until they are
+            # destroyed (the library requires the index to outlive them): close them first
+            for kind in ("learned", "plan", "hash"):
+                for o in list(_live[kind]):
+                    if getattr(o, "index", None) is self:
+                        o.close()
             lib().efg_index_destroy(self._h)
             self._h = C.c_void_p()
 

@@ -86,3 +86,35 @@ def test_every_entry_point_refuses_null_arguments(efg):
         else:
             f.restype = None
             f(*zeros)
+
+
+def test_index_close_destroys_its_dependents_first(efg, monkeypatch):
+    """Closing an Index first closes the plans, learned models and hash tables built on it (the
+    library requires the index to outlive them); objects of another index stay open.  The C
+    library is replaced by a recorder, so this runs without a GPU."""
+    import ctypes as C
+    calls = []
+
+    class FakeLib:
+        def __getattr__(self, name):
+            return lambda h: calls.append((name, h.value if isinstance(h, C.c_void_p) else h))
+
+    monkeypatch.setattr(efg, "lib", lambda: FakeLib())
+    idx, other = object.__new__(efg.Index), object.__new__(efg.Index)
+    idx._h, other._h = C.c_void_p(0x1000), C.c_void_p(0x2000)
+    made = []
+    for cls, h, owner in ((efg.Learned, 0x11, idx), (efg.SearchPlan, 0x12, idx), (efg.HashTables, 0x13, idx),
+                          (efg.HashTables, 0x23, other)):
+        o = object.__new__(cls)
+        o.index, o._h = owner, C.c_void_p(h)
+        efg._live[{"Learned": "learned", "SearchPlan": "plan", "HashTables": "hash"}[cls.__name__]].add(o)
+        made.append(o)
+    idx.close()
+    assert calls == [("efg_learned_destroy", 0x11), ("efg_search_plan_destroy", 0x12),
+                     ("efg_hash_destroy", 0x13), ("efg_index_destroy", 0x1000)]
+    idx.close()                                   # idempotent
+    assert len(calls) == 4
+    other.close()
+    assert calls[4:] == [("efg_hash_destroy", 0x23), ("efg_index_destroy", 0x2000)]
+    for o in made:
+        efg._live["learned"].discard(o), efg._live["plan"].discard(o), efg._live["hash"].discard(o)

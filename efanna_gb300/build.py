@@ -55,10 +55,12 @@ def _compile(src: str, phase_clocks: bool = False) -> str:
 
 def build(verbose: bool = False, phase_clocks: bool = False) -> str:
     """Builds the library; ``phase_clocks`` builds the diagnostic one (PHASE_LIB) instead."""
-    out_dir, lib = (PHASE_OUT_DIR, PHASE_LIB) if phase_clocks else (OUT_DIR, LIB)
-    os.makedirs(out_dir, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda src: _compile(src, phase_clocks), SOURCES))
+    lib = PHASE_LIB if phase_clocks else LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if phase_clocks:
+        os.makedirs(PHASE_OUT_DIR, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:  # only search.cu reads the macro
+        objs = list(ex.map(lambda src: _compile(src, phase_clocks and src == "search.cu"), SOURCES))
     if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(o) for o in objs):
         return lib
     cmd = [nvcc(), "-shared", "-o", lib] + objs + ARCH + ["-lcudart", "-lpthread"]

@@ -118,3 +118,19 @@ def test_index_close_destroys_its_dependents_first(efg, monkeypatch):
     assert calls[4:] == [("efg_hash_destroy", 0x23), ("efg_index_destroy", 0x2000)]
     for o in made:
         efg._live["learned"].discard(o), efg._live["plan"].discard(o), efg._live["hash"].discard(o)
+
+
+def test_phase_clock_build_exports_the_same_symbols(efg):
+    """The diagnostic build (per-phase cycle counters in the search kernel) compiles beside the
+    product library, under its own name, with the same entry points."""
+    import shutil
+    from efanna_gb300 import build as B
+    if not (os.environ.get("NVCC") or shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
+        pytest.skip("nvcc not available")
+    lib = B.build(phase_clocks=True)
+    assert lib == B.PHASE_LIB and lib != B.LIB
+    syms = []
+    for path in (B.LIB, lib):
+        out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+        syms.append(set(re.findall(r" T (efg_[a-z0-9_]+)", out)))
+    assert syms[0] == syms[1] and set(declared()) <= syms[1]

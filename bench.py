@@ -36,6 +36,14 @@ sys.path.insert(0, ROOT)
 METRIC = "graph build s & QPS at recall@10>=0.95, 1xGB300: plain FP32 vs BF16+learned"
 GRAPH = dict(trees=8, merge_level=8, epochs=8, check=25, L=30, K=10, S=10)
 SEARCH_TREES = 16
+
+
+def workload(n: int, nq: int) -> str:
+    """The workload's name with the sizes actually run (1M x 128 and 10k queries by default)."""
+    def size(v):
+        return "%gM" % (v / 1e6) if v % 1_000_000 == 0 else "%gk" % (v / 1e3) if v % 1000 == 0 else str(v)
+    return ("%s x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), 16 search trees, "
+            "%s queries, k=10" % (size(n), size(nq)))
 CONFIG_POINT = (4, 1200, 200)  # the reference configuration's epochs / pool / extend
 # search settings (epochs, pool, extend) in ascending cost; the first reaching the target recall is
 # the operating point.  Index 4 is where the plain FP32 search with 16 trees reaches it on this
@@ -276,8 +284,7 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(f32["per_step_ms"], 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded integer-valued Gaussian mixture)",
-        "config": {"workload": "1M x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), "
-                               "16 search trees, 10k queries, k=10",
+        "config": {"workload": workload(args.n, nq),
                    "n": args.n, "dim": 128, "queries": nq, "k": 10, "search_trees": SEARCH_TREES,
                    "operating_point": point_of(f32),
                    "config_point": {"epochs": CONFIG_POINT[0], "pool": CONFIG_POINT[1], "extend": CONFIG_POINT[2],
@@ -721,6 +728,8 @@ def run_reference(args):
     t0 = time.perf_counter()
     rc, gs, _, _ = O.build_graph(x, p, O.OMP)
     build_s = time.perf_counter() - t0
+    if rc != 0:  # the reference program exits here too (merge level deeper than a tree leaf)
+        raise SystemExit("reference arm: the graph build failed with status %d at n = %d" % (rc, args.n))
     t0 = time.perf_counter()
     forest = O.Forest.build(x, SEARCH_TREES, mode=O.OMP)
     trees_s = time.perf_counter() - t0
@@ -744,8 +753,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded integer-valued Gaussian mixture)",
-            "config": {"workload": "1M x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10), "
-                                   "16 search trees, 10k queries, k=10",
+            "config": {"workload": workload(args.n, args.nq),
                        "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2]}},
             "build": {"graph_build_s": round(build_s, 3), "search_trees16_s": round(trees_s, 3), "status": rc},
             "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": cores, "kind": "port",

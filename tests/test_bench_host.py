@@ -43,3 +43,35 @@ def test_peaks_prefers_the_measured_file(tmp_path, monkeypatch):
     assert bench.peaks() == (6800.0, "fallback")
     (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6791.7, "bf16_tflops": 1900}))
     assert bench.peaks() == (6791.7, "measured")
+
+
+def _bench(*args):
+    import subprocess
+    import sys
+    from conftest import ROOT
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + list(args), capture_output=True,
+                          text=True, timeout=600, cwd=ROOT)
+
+
+def test_reference_arm_line():
+    """`bench.py --impl reference` (the OpenMP restatement of the reference on the host cores) at a
+    small size: one JSON line with the arm's keys, the workload named by the sizes run."""
+    r = _bench("--impl", "reference", "--n", "100000", "--nq", "200", "--steps", "3", "--warmup", "3",
+               "--cpu-queries", "50")
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "queries/s" and line["value"] > 0
+    assert line["steps"] == 3 and line["warmup"] == 3 and line["higher_is_better"] is True
+    assert line["config"]["workload"].startswith("100k x 128 FP32") and "200 queries" in line["config"]["workload"]
+    assert line["build"]["status"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_fails_when_the_build_fails():
+    """Merge level 8 is deeper than the trees of a 20k-point base: the build's status ends the arm
+    with an error instead of timing a search on no graph."""
+    r = _bench("--impl", "reference", "--n", "20000", "--nq", "100", "--steps", "3", "--warmup", "3")
+    assert r.returncode != 0
+    assert "graph build failed with status 3" in r.stderr

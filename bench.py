@@ -119,6 +119,33 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def exact_knn_host(x: np.ndarray, q: np.ndarray, k: int = 10, exclude: np.ndarray | None = None) -> np.ndarray:
+    """Exact k-NN on the host cores, ordered by (distance, id) as the GPU's ground truth.  The data
+    are integers in [0, 255] with d = 128, so the FP32 Gram form ||x||^2 + ||q||^2 - 2 x.q is exact
+    (every partial sum is an integer below 2^24); distance * 2^20 + id is then an exact FP64 key
+    (n < 2^20 rows).  exclude[i], when given, is the base row that query i must skip (itself)."""
+    xf = x.astype(np.float32)
+    sq = (xf * xf).sum(1)
+    ids = np.arange(len(x), dtype=np.float64)
+    out = np.zeros((len(q), k), np.int64)
+    for b in range(0, len(q), 256):
+        qb = q[b:b + 256].astype(np.float32)
+        qs = (qb * qb).sum(1)
+        best_key = np.full((len(qb), 0), 0.0)
+        for c in range(0, len(x), 200_000):
+            d = qs[:, None] + sq[None, c:c + 200_000] - 2 * (qb @ xf[c:c + 200_000].T)
+            key = d.astype(np.float64) * 1048576.0 + ids[None, c:c + 200_000]
+            if exclude is not None:
+                r = exclude[b:b + 256] - c
+                hit = (r >= 0) & (r < key.shape[1])
+                key[np.nonzero(hit)[0], r[hit]] = np.inf
+            part = np.partition(key, k - 1, axis=1)[:, :k] if key.shape[1] > k else key
+            best_key = np.concatenate([best_key, part], 1)
+        best_key.sort(1)
+        out[b:b + 256] = np.round(np.fmod(best_key[:, :k], 1048576.0)).astype(np.int64)
+    return out
+
+
 def make_data(n, nq):
     from efanna_gb300 import datasets
     x = datasets.mixture_u8(n, 128, seed=0)
@@ -150,6 +177,15 @@ def run_gpu(args):
         build_s.append(time.perf_counter() - t0)
     bst = idx.build_stats()
     graph = idx.graph()
+    # the same build from host rows, as the reference's buildIndex is called: the index's copy of the
+    # 512 MB base to the device is inside the timed region
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx_h = E.Index(x, E.IndexParams(**GRAPH))
+    idx_h.build_index()
+    torch.cuda.synchronize()
+    host_build_s = time.perf_counter() - t0
+    idx_h.close()
     t0 = time.perf_counter()
     idx.build_trees(SEARCH_TREES)
     torch.cuda.synchronize()
@@ -292,6 +328,7 @@ def run_gpu(args):
                    "ladder": f32["ladder"], "l2": "inputs larger than L2 (512 MB base), no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "build": {"graph_build_s": round(min(build_s), 4), "graph_build_s_runs": [round(b, 4) for b in build_s],
+                  "graph_build_host_input_s": round(host_build_s, 4),
                   "trees_ms": round(bst.trees_ms, 2), "init_ms": round(bst.init_ms, 2),
                   "refine_ms": round(bst.refine_ms, 2), "join_pairs": int(bst.join_pairs),
                   "graph_recall@10": round(graph_recall, 4), "search_trees16_s": round(trees_s, 4)},
@@ -743,7 +780,12 @@ def run_reference(args):
                         trees=SEARCH_TREES, mode=O.OMP, threads=cores)
 
     for w in range(args.warmup):
-        step(0)
+        res0 = step(0)
+    # the arm's own recall (outside the timed region): its search on the first sample against the exact
+    # 10-NN, and its graph on sampled rows against their exact neighbours (self excluded)
+    search_recall = recall(res0, exact_knn_host(x, q[:ns]))
+    rows = np.sort(np.random.default_rng(5).choice(args.n, min(args.n, args.graph_rows), replace=False))
+    graph_recall = recall(gs[rows], exact_knn_host(x, x[rows], exclude=rows))
     t0 = time.perf_counter()
     for s in range(args.steps):
         step((s * ns) % max(1, len(q) - ns + 1))
@@ -755,7 +797,9 @@ def run_reference(args):
             "data": "synthetic (seeded integer-valued Gaussian mixture)",
             "config": {"workload": workload(args.n, args.nq),
                        "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2]}},
-            "build": {"graph_build_s": round(build_s, 3), "search_trees16_s": round(trees_s, 3), "status": rc},
+            "build": {"graph_build_s": round(build_s, 3), "search_trees16_s": round(trees_s, 3), "status": rc,
+                      "graph_recall@10": round(graph_recall, 4), "graph_recall_rows": len(rows)},
+            "recall@10": round(search_recall, 4), "recall_queries": ns,
             "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": cores, "kind": "port",
                              "sample": "%d queries per step; index built by the OpenMP restatement of the "
                                        "reference on the same host" % ns, "cpu_model": cpu_model(),
@@ -773,6 +817,7 @@ def main():
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--nq", type=int, default=10_000)
     ap.add_argument("--cpu-queries", type=int, default=1000)
+    ap.add_argument("--graph-rows", type=int, default=2000, help="sampled rows for the graph recall")
     ap.add_argument("--point", type=int, nargs=3, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")

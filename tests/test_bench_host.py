@@ -64,6 +64,8 @@ def test_reference_arm_line():
     assert line["steps"] == 3 and line["warmup"] == 3 and line["higher_is_better"] is True
     assert line["config"]["workload"].startswith("100k x 128 FP32") and "200 queries" in line["config"]["workload"]
     assert line["build"]["status"] == 0
+    assert 0.9 < line["build"]["graph_recall@10"] <= 1.0 and line["build"]["graph_recall_rows"] == 2000
+    assert 0.8 < line["recall@10"] <= 1.0 and line["recall_queries"] == 50
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}

@@ -149,6 +149,7 @@ def lib():
         "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
         "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
         "efg_set_search_precision": (i32, [vp, i32]),
+        "efg_set_search_candidate_cap": (i32, [vp, u32]),
         "efg_screen_distances": (i32, [vp, i32, vp, u64, u64, vp, u32, vp, vp]),
         "efg_knn_search": (i32, [vp, f32p, u64, u32, u64, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_device": (i32, [vp, vp, u64, u64, u32, vp, vp]),
@@ -287,6 +288,10 @@ class Index:
         if code is None:
             raise ValueError("precision must be 'fp32', 'bf16' or 'fp8'")
         _check(lib().efg_set_search_precision(self._h, code))
+
+    def set_search_candidate_cap(self, cap: int) -> None:
+        """Bound on the nnexp search's per-query candidate buffer (0: the worst case, the default)."""
+        _check(lib().efg_set_search_candidate_cap(self._h, cap))
 
     def screen_distances_device(self, precision: str, q_ptr: int, nq: int, row_stride: int, ids_ptr: int, m: int,
                                 out_ptr: int, stream: int = 0):

@@ -358,6 +358,12 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
   return EFG_OK;
 }
 
+int efg_set_search_candidate_cap(efg_index* idx, uint32_t cap) {
+  if (!idx) return fail(EFG_ERR_ARG, "null index");
+  idx->candidate_cap = cap;
+  return EFG_OK;
+}
+
 int efg_set_search_precision(efg_index* idx, int precision) {
   if (!idx) return fail(EFG_ERR_ARG, "null index");
   if (precision != EFG_PRECISION_FP32 && precision != EFG_PRECISION_BF16 && precision != EFG_PRECISION_FP8)

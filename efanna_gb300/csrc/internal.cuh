@@ -147,6 +147,7 @@ struct efg_index {
   efg::DevBuf<uint32_t> kg_bits;
   efg::DevBuf<efg_query_params> qp_buf;  // per-query parameters of a host batch
   int search_threads = 0;                  // nnexp block size forced by a plan's autotuner (0: by occupancy)
+  uint32_t candidate_cap = 0;              // bound on the nnexp candidate buffer (0: extend_to x degree)
 };
 
 namespace efg {

@@ -252,6 +252,7 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
                  int32_t* d_out, uint64_t* d_keys, cudaStream_t s, int* launches, const efg_query_params* d_params,
                  const uint32_t* d_nq, const uint32_t* d_seeds) {
   *launches = 0;
+  cfg.ids_cap = idx->candidate_cap;  // layout() reads it as a bound, then sets the buffer's size
   if (cfg.T > 256) return fail(EFG_ERR_ARG, "at most 256 search trees");
   if (cfg.lsize >= 65536) return fail(EFG_ERR_ARG, "pool too large for the tree descent");
   cfg.emit_pool = d_keys ? 1 : 0;

@@ -12,7 +12,7 @@ struct SearchCfg {
   uint32_t ht_mig;      // (when enabled) into a table of mig_size slots, the worst case
   uint32_t mig_size;
   uint32_t ht_global;   // visited set in a per-CTA slice of global scratch
-  uint32_t ids_cap;     // candidate id buffer (u32 entries)
+  uint32_t ids_cap;     // candidate id buffer (u32 entries); on entry to layout(): a bound, 0 = none
   uint32_t res_cap;     // power of two >= result_size
   uint32_t nseq;        // T * lsize leaf slots
   // shared-memory byte offsets

@@ -115,6 +115,13 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
 #define EFG_PRECISION_BF16 1
 #define EFG_PRECISION_FP8 2  /* e4m3 copy with one FP32 scale per row (max|x| / 448); same re-rank */
 int efg_set_search_precision(efg_index* idx, int precision);
+/* Bound on the nnexp search's per-query candidate buffer (no reference counterpart; the reference's
+ * candidate vector grows without bound).  0, the default, sizes it for the worst case of one
+ * expansion epoch, extend_to x graph degree, which cannot overflow.  A smaller bound needs less
+ * shared memory per query; it never goes below the pool size or the tree-descent frontier.  When an
+ * epoch of some query appends more new candidates than the buffer holds, the extra ones are dropped
+ * on the device and the search call returns EFG_ERR_DEVICE_LIMIT ("candidate buffer overflow"). */
+int efg_set_search_candidate_cap(efg_index* idx, uint32_t cap);
 /* The search's screening distances for given pairs: query q (device memory, row_stride floats apart)
  * against ids d_ids[q*m .. q*m + m) (m <= 4096), in `precision`; FP32 results into d_out (nq x m).
  * Used to state each precision's distance error against an FP64 reference. */

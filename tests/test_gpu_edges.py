@@ -1,10 +1,13 @@
 """Edge cases of the path against the oracle's canonical restatement: exact duplicates (distance
 ties everywhere), dimensions that are not multiples of the vector widths, the smallest base the
 build accepts, empty query batches, queries equal to base points, and graphs with rows of different
-lengths (loaded from a file)."""
+lengths (loaded from a file), and a device-side limit made to fire."""
+import os
+
 import numpy as np
 import pytest
 
+from conftest import GOLDEN, load_golden
 from efanna_gb300 import datasets, io
 
 pytestmark = pytest.mark.gpu
@@ -128,3 +131,30 @@ def test_variable_degree_graph_from_file(efg, oracle_lib, tmp_path):
         kref, _, _ = O.search_kgraph(x, forest, gp, gi, q, k=10, epochs=pt[0], init_num=pt[1], extend_to=pt[2],
                                      trees=4, mode=O.CANON, threads=4)
         assert np.array_equal(idx.knn_search(10, q), kref), pt
+
+
+def test_candidate_buffer_overflow_returns_device_limit(efg):
+    """A device-side limit made to fire without any fault: the candidate buffer bounded below what
+    one expansion epoch appends (extend = pool = 600 over a degree-10 graph appends up to 6000
+    candidates; the bound is clamped up to the pool and the descent frontier, under 1000 here).
+    The kernel drops the extra candidates, sets its error word, and the call returns
+    EFG_ERR_DEVICE_LIMIT; with the bound lifted the same index searches as before."""
+    g = load_golden("mid_d128")
+    x = g["base"].astype(np.float32)
+    q = g["queries"].astype(np.float32)
+    idx = efg.Index(x, efg.IndexParams(trees=8))
+    idx.load_trees(os.path.join(GOLDEN, "mid_d128.trees"))
+    idx.load_graph(os.path.join(GOLDEN, "mid_d128.graph"))
+    idx.set_search_params(4, 600, 600, 8)
+    before = idx.knn_search(10, q)
+    idx.set_search_candidate_cap(1)
+    with pytest.raises(efg.EfannaError) as e:
+        idx.knn_search(10, q)
+    assert e.value.code == efg.EFG_ERR_DEVICE_LIMIT and "candidate buffer overflow" in str(e.value)
+    idx.set_search_candidate_cap(0)
+    assert np.array_equal(idx.knn_search(10, q), before)
+    idx.set_search_params(4, 600, 100, 8)  # 100 x 10 items per epoch fit a 1000-entry bound
+    ref = idx.knn_search(10, q)
+    idx.set_search_candidate_cap(1000)
+    assert np.array_equal(idx.knn_search(10, q), ref)
+    idx.close()

@@ -167,6 +167,8 @@ def lib():
         "efg_l2_pairs": (i32, [vp, u64, u32, u64, vp, vp, u64, vp, vp]),
         "efg_brute_force_knn": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_brute_force_knn_fp32": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_brute_force_knn_split": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_knn_search_batch": (i32, [vp, f32p, u64, u32, u64, vp, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
         "efg_knn_search_seeded_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, u32, i32, vp, vp]),
@@ -611,10 +613,14 @@ def l2_pairs_device(base_ptr: int, n: int, dim: int, row_stride: int, a_ptr: int
 
 def brute_force_knn_device(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int, q_stride: int,
                            k: int, ids_ptr: int, dists_ptr: int = 0, exclude_self: bool = False, first_row: int = 0,
-                           stream: int = 0) -> None:
-    _check(lib().efg_brute_force_knn(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(q_ptr), nq, q_stride, k,
-                                     int(exclude_self), first_row, C.c_void_p(ids_ptr),
-                                     C.c_void_p(dists_ptr or None), C.c_void_p(stream)))
+                           stream: int = 0, screening: str = "auto") -> None:
+    """Exact k-NN (efg_brute_force_knn).  screening: 'auto' (tensor cores for k <= 104), 'fp32'
+    (the FP32 CUDA-core kernel) or 'split' (tensor cores with the hi + lo split forced)."""
+    fn = {"auto": "efg_brute_force_knn", "fp32": "efg_brute_force_knn_fp32",
+          "split": "efg_brute_force_knn_split"}[screening]
+    _check(getattr(lib(), fn)(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(q_ptr), nq, q_stride, k,
+                              int(exclude_self), first_row, C.c_void_p(ids_ptr), C.c_void_p(dists_ptr or None),
+                              C.c_void_p(stream)))
 
 
 def brute_force_knn_device_noalloc(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int,

@@ -71,6 +71,15 @@ static constexpr int BF_THREADS = 256;  // rows per step
 static constexpr int BF_CAP = 1024;     // candidate buffer per query
 static constexpr int BF_MARGIN = 16;    // extra candidates kept for the FP64 re-rank
 
+// Base chunks of the FP32 kernel: enough blocks for eight per SM, chunks of at least 2048 rows, and
+// at most 4096 keys per query for the merge.
+static uint64_t bf_chunks(uint64_t n, uint64_t nq, uint32_t K2) {
+  uint64_t qblocks = (nq + BF_QB - 1) / BF_QB;
+  uint64_t want = std::max<uint64_t>(1, (152ull * 8 + qblocks - 1) / qblocks);
+  uint64_t nchunks = std::min<uint64_t>(want, std::max<uint64_t>(1, n / 2048));
+  return std::min<uint64_t>(nchunks, std::max<uint64_t>(1, 4096 / K2));
+}
+
 // Sorts `n` (power of two) keys in shared memory with the whole block.
 __device__ void block_bitonic_sort(uint64_t* keys, uint32_t n) {
   for (uint32_t k = 2; k <= n; k <<= 1) {
@@ -304,39 +313,23 @@ __global__ void bf_merge_kernel(const float* __restrict__ base, uint32_t dim, ui
   }
 }
 
-int brute_force_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
-                    uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+// Launches the merge of the per-(query, chunk) lists `part` (nq x nchunks x K2 keys): per query the
+// K2 smallest keys, re-ranked in FP64, of which the k first go to ids (and dists).
+int bf_merge_launch(const float* base, uint32_t dim, uint32_t ld, const float* q, uint64_t nq, uint32_t qld,
+                    uint32_t k, uint32_t K2, uint32_t nchunks, const uint64_t* part, int32_t* ids, float* dists,
                     cudaStream_t s) {
-  if (nq == 0) return EFG_OK;
-  uint32_t K2 = std::min<uint64_t>(k + BF_MARGIN, n);
-  uint64_t qblocks = (nq + BF_QB - 1) / BF_QB;
-  uint64_t want = std::max<uint64_t>(1, (152ull * 8 + qblocks - 1) / qblocks);
-  uint64_t nchunks = std::min<uint64_t>(want, std::max<uint64_t>(1, n / 2048));
-  nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, 4096 / K2));
-  uint64_t chunk = (n + nchunks - 1) / nchunks;
-  nchunks = (n + chunk - 1) / chunk;
-  uint64_t* part = nullptr;
-  EFG_CUDA(cudaMallocAsync((void**)&part, nq * nchunks * K2 * sizeof(uint64_t), s));
-  uint32_t ld4 = (dim + 3) / 4;
-  size_t smem = (size_t)BF_QB * ld4 * 16 + (size_t)BF_QB * BF_CAP * 8;
-  if (smem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)qblocks, (unsigned)nchunks);
-  bf_chunk_kernel<<<grid, BF_THREADS, smem, s>>>(base, n, dim, ld, q, nq, qld, K2, chunk, exclude_self, first_row,
-                                                 part);
-  EFG_CUDA(cudaGetLastError());
-  uint32_t tot = (uint32_t)(nchunks * K2), p2 = 1;
+  uint32_t tot = nchunks * K2, p2 = 1;
   while (p2 < tot) p2 <<= 1;
   uint32_t wpb = p2 <= 2048 ? 4 : 1;
   size_t msmem = (size_t)wpb * p2 * 8 + (size_t)wpb * K2 * 8;
   if (msmem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem));
-  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2,
-                                                                            (uint32_t)nchunks, part, ids, dists);
+  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2, nchunks,
+                                                                            part, ids, dists);
   EFG_CUDA(cudaGetLastError());
-  EFG_CUDA(cudaFreeAsync(part, s));
   return EFG_OK;
 }
 
-// The same two kernels with caller-provided scratch for the per-(query, chunk) candidate lists:
+// The FP32 kernels with caller-provided scratch for the per-(query, chunk) candidate lists:
 // `part` holds part_cap keys; the base is cut into as many chunks as fit (at least one).  Every
 // slot the merge reads is written by bf_chunk_kernel first, so the scratch needs no clearing.
 int brute_force_knn_in(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
@@ -348,29 +341,36 @@ int brute_force_knn_in(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
     return fail(EFG_ERR_ARG, "brute force needs " + std::to_string(nq * K2) + " scratch entries (queries x (k+" +
                                  std::to_string(BF_MARGIN) + ")); the built-in scratch holds " +
                                  std::to_string(part_cap));
-  uint64_t qblocks = (nq + BF_QB - 1) / BF_QB;
-  uint64_t want = std::max<uint64_t>(1, (152ull * 8 + qblocks - 1) / qblocks);
-  uint64_t nchunks = std::min<uint64_t>(want, std::max<uint64_t>(1, n / 2048));
-  nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, 4096 / K2));
+  uint64_t nchunks = bf_chunks(n, nq, K2);
   nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, part_cap / (nq * K2)));
   uint64_t chunk = (n + nchunks - 1) / nchunks;
   nchunks = (n + chunk - 1) / chunk;
   uint32_t ld4 = (dim + 3) / 4;
   size_t smem = (size_t)BF_QB * ld4 * 16 + (size_t)BF_QB * BF_CAP * 8;
   if (smem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)qblocks, (unsigned)nchunks);
+  dim3 grid((unsigned)((nq + BF_QB - 1) / BF_QB), (unsigned)nchunks);
   bf_chunk_kernel<<<grid, BF_THREADS, smem, s>>>(base, n, dim, ld, q, nq, qld, K2, chunk, exclude_self, first_row,
                                                  part);
   EFG_CUDA(cudaGetLastError());
-  uint32_t tot = (uint32_t)(nchunks * K2), p2 = 1;
-  while (p2 < tot) p2 <<= 1;
-  uint32_t wpb = p2 <= 2048 ? 4 : 1;
-  size_t msmem = (size_t)wpb * p2 * 8 + (size_t)wpb * K2 * 8;
-  if (msmem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem));
-  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2,
-                                                                            (uint32_t)nchunks, part, ids, dists);
-  EFG_CUDA(cudaGetLastError());
-  return EFG_OK;
+  return bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, (uint32_t)nchunks, part, ids, dists, s);
+}
+
+// The FP32 path with its scratch from the stream-ordered allocator: as many chunks as the
+// occupancy target asks for.
+int brute_force_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                    uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                    cudaStream_t s) {
+  if (nq == 0) return EFG_OK;
+  uint32_t K2 = std::min<uint64_t>(k + BF_MARGIN, n);
+  uint64_t nchunks = bf_chunks(n, nq, K2);
+  uint64_t chunk = (n + nchunks - 1) / nchunks;
+  nchunks = (n + chunk - 1) / chunk;
+  const uint64_t cap = nq * nchunks * K2;
+  uint64_t* part = nullptr;
+  EFG_CUDA(cudaMallocAsync((void**)&part, cap * sizeof(uint64_t), s));
+  int rc = brute_force_knn_in(base, n, dim, ld, q, nq, qld, k, exclude_self, first_row, ids, dists, part, cap, s);
+  cudaFreeAsync(part, s);
+  return rc;
 }
 
 }  // namespace efg

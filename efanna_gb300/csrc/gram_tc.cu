@@ -1,0 +1,583 @@
+// Exact k-NN screening on the fifth-generation tensor cores (tcgen05, sm_103a).
+//
+// Matrix::brute_force_search (general/matrix.hpp:57-68) ranks every base row by its squared L2
+// distance to the query.  Written as ||q||^2 + ||x||^2 - 2 q.x, the distances of a block of
+// queries against a block of base rows are one dense Gram contraction, which this file runs as
+// BF16 tcgen05.mma tiles accumulated in FP32 in tensor memory (TMEM):
+//
+//   * queries and base rows are converted once per call to BF16 rows padded to a multiple of 64
+//     values (128 bytes, one 128-byte-swizzle row), together with their FP32 squared norms.  Data
+//     whose values BF16 holds exactly (the integer-valued configurations: values in [0, 255]) use
+//     one product per tile, and then every product and every FP32 partial sum is an exact integer
+//     below 2^24, so the screened distances equal the exact ones.  Other data are split as
+//     x = hi + lo (two BF16 values) and each tile accumulates hi.hi + hi.lo + lo.hi, which leaves
+//     an error near 2^-16 of |q.x| instead of 2^-8.
+//   * a CTA owns one work item at a time: 128 queries (the MMA's M, one TMEM lane each) against
+//     one chunk of base rows, walked in tiles of 128 rows (N).  Warp 0 streams the operand
+//     k-blocks into a ring of shared-memory stages with cp.async.bulk.tensor (TMA, 128-byte
+//     swizzle), one (query block, base block) pair per stage -- in the split form three pairs per
+//     k-block: (hi, hi), (hi, lo), (lo, hi); one thread of warp 1 issues the MMAs (K = 16 each) into one of two TMEM
+//     accumulators and commits them to mbarriers; warps 2-5 read the other accumulator with
+//     tcgen05.ld, one query per thread, turn each Gram value into a distance and keep the
+//     query's best K2 = k + 16 (distance, id) keys of the chunk.  The two accumulators let the
+//     MMAs of tile t + 1 run while tile t is being screened.
+//   * each thread's candidates first go to a small buffer in shared memory; when any lane's buffer
+//     nears full, the warp merges its buffers into the threads' sorted lists and tightens the
+//     thresholds, so the per-value work is one FMA, one compare and (rarely) one store.
+//
+// The chunks' lists are the same per-(query, chunk) lists the FP32 kernel writes (distance.cu);
+// the same merge kernel then re-ranks the K2 survivors of each query in FP64.  Every wait on an
+// mbarrier is bounded: a wait that runs out sets an error word and the CTA leaves its loops,
+// drains its tensor-core work and frees its TMEM; the host turns the word into
+// EFG_ERR_DEVICE_LIMIT.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace efg {
+
+int bf_merge_launch(const float* base, uint32_t dim, uint32_t ld, const float* q, uint64_t nq, uint32_t qld,
+                    uint32_t k, uint32_t K2, uint32_t nchunks, const uint64_t* part, int32_t* ids, float* dists,
+                    cudaStream_t s);
+
+namespace {
+
+constexpr uint32_t TM = 128;           // queries per tile (MMA M, TMEM lanes)
+constexpr uint32_t TN = 128;           // base rows per tile (MMA N, TMEM columns per accumulator)
+constexpr uint32_t TKB = 64;           // BF16 values per k-block: one 128-byte swizzle row
+constexpr uint32_t PART = TM * TKB * 2;  // bytes of one 128 x 64 BF16 operand block (16 KiB)
+constexpr uint32_t BUF = 32;           // candidate buffer slots per thread
+constexpr uint32_t THREADS = 192;      // warp 0 TMA, warp 1 MMA (+TMEM), warps 2-5 screening
+constexpr uint32_t MAX_STAGES = 8;
+constexpr uint32_t TMEM_COLS = 2 * TN;  // two FP32 accumulators of 128 columns
+constexpr unsigned long long WAIT_CYCLES = 4000000000ull;  // about 2 s at 2 GHz
+
+// instruction descriptor of tcgen05.mma.kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
+// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((TN >> 3) << 17) | ((TM >> 4) << 24);
+
+struct TcArgs {
+  const float* qnorm;  // nq FP32 squared norms
+  const float* xnorm;  // squared norms of the base rows, +inf past n (rounded up to a tile)
+  uint64_t* part;      // nq x nchunks x K2 keys
+  int* err;
+  uint64_t n, chunk, first_row;
+  uint32_t nq, qtiles, nchunks, K2, kblocks, terms, stages, exclude_self;
+  uint32_t o_list, o_buf;  // byte offsets of the lists and buffers in dynamic shared memory
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the phase of `parity` to complete; false when the CTA is aborting or the wait ran out
+// (which also starts the abort).
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err) {
+  unsigned long long t0 = clock64();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 127) == 127) {
+      if (*abort_flag) return false;
+      if (clock64() - t0 > WAIT_CYCLES) {
+        *abort_flag = 1;
+        atomicOr(err, 1);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a 128-row block of K-major BF16 rows, 128 bytes per row, in
+// the 128-byte swizzle layout TMA writes: 8-row groups 1024 bytes apart (stride byte offset),
+// descriptor version 1 (bits 46-47), swizzle mode 2 = 128 bytes (bits 61-63).  The block must
+// start on a 1024-byte boundary; the k-th 16-value slice starts 32 * k bytes further.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 lanes x 32 consecutive FP32 columns (two x16 loads, one wait): thread i of the warp receives
+// the 32 values of TMEM lane (lane base + i) starting at the address's column.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr + 16));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Merges a thread's buffered keys into its sorted list of at most K2 keys.  Lists and buffers are
+// slot-major with a stride of 128 (the screening threads), so the threads of a warp touch
+// consecutive words.
+__device__ __forceinline__ void merge_buffer(uint64_t* list, const uint64_t* buf, uint32_t t, uint32_t K2,
+                                             uint32_t& lcnt, uint32_t& bcnt, float& thr) {
+  for (uint32_t i = 0; i < bcnt; ++i) {
+    uint64_t key = buf[i * TM + t];
+    if (lcnt == K2 && key >= list[(K2 - 1) * TM + t]) continue;
+    uint32_t j = lcnt < K2 ? lcnt : K2 - 1;  // a full list drops its last key
+    while (j > 0) {
+      uint64_t prev = list[(j - 1) * TM + t];
+      if (prev <= key) break;
+      list[j * TM + t] = prev;
+      --j;
+    }
+    list[j * TM + t] = key;
+    if (lcnt < K2) ++lcnt;
+  }
+  bcnt = 0;
+  if (lcnt == K2) thr = __uint_as_float((uint32_t)(list[(K2 - 1) * TM + t] >> 32));
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    tc_knn_kernel(const __grid_constant__ CUtensorMap mq_hi, const __grid_constant__ CUtensorMap mq_lo,
+                  const __grid_constant__ CUtensorMap mx_hi, const __grid_constant__ CUtensorMap mx_lo,
+                  const TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_full[MAX_STAGES], bar_empty[MAX_STAGES], bar_tfull[2], bar_tempty[2],
+      bar_drain;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_sh;
+
+  // stages start on a 1024-byte boundary (the swizzle pattern repeats every 1024 bytes)
+  const uint32_t raw = smem_addr(smem_raw);
+  const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+  unsigned char* smem = smem_raw + pad;
+  const uint32_t sbase = raw + pad;
+  const uint32_t stage_bytes = 2 * PART;  // a query block and a base block
+  const uint32_t steps = a.kblocks * a.terms;  // stages per tile
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < a.stages; ++s) {
+      mbar_init(smem_addr(&bar_full[s]), 1);
+      mbar_init(smem_addr(&bar_empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_addr(&bar_tfull[b]), 1);
+      mbar_init(smem_addr(&bar_tempty[b]), TM);
+    }
+    mbar_init(smem_addr(&bar_drain), 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {  // the whole warp allocates the two accumulators
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_sh)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = tmem_base_sh;
+  volatile int* abort_flag = &abort_sh;
+  const uint32_t items = a.qtiles * a.nchunks;
+  bool mma_issued = false;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- TMA producer (one lane)
+    if (lane == 0) {
+      uint32_t s = 0, ph = 0;
+      bool ok = true;
+      for (uint32_t w = blockIdx.x; ok && w < items; w += gridDim.x) {
+        const uint32_t chunk = w / a.qtiles, qt = w % a.qtiles;
+        const uint64_t r0 = (uint64_t)chunk * a.chunk, r1 = min(a.n, r0 + a.chunk);
+        const uint32_t ntiles = (uint32_t)((r1 - r0 + TN - 1) / TN);
+        for (uint32_t t = 0; ok && t < ntiles; ++t) {
+          for (uint32_t step = 0; step < steps; ++step) {
+            if (!mbar_wait(smem_addr(&bar_empty[s]), ph ^ 1u, abort_flag, a.err)) {
+              ok = false;
+              break;
+            }
+            const uint32_t kb = step / a.terms, term = step - kb * a.terms;  // term 0 (hi,hi), 1 (hi,lo), 2 (lo,hi)
+            const uint32_t fb = smem_addr(&bar_full[s]);
+            mbar_expect_tx(fb, stage_bytes);
+            const uint32_t st = sbase + s * stage_bytes;
+            const int x = (int)(kb * TKB), yq = (int)(qt * TM), yx = (int)(r0 + (uint64_t)t * TN);
+            tma_load_2d(st, term == 2 ? &mq_lo : &mq_hi, fb, x, yq);
+            tma_load_2d(st + PART, term == 1 ? &mx_lo : &mx_hi, fb, x, yx);
+            if (++s == a.stages) {
+              s = 0;
+              ph ^= 1u;
+            }
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- MMA issuer (one lane)
+    if (lane == 0) {
+      uint32_t s = 0, ph = 0, tcount = 0;
+      bool ok = true;
+      for (uint32_t w = blockIdx.x; ok && w < items; w += gridDim.x) {
+        const uint32_t chunk = w / a.qtiles;
+        const uint64_t r0 = (uint64_t)chunk * a.chunk, r1 = min(a.n, r0 + a.chunk);
+        const uint32_t ntiles = (uint32_t)((r1 - r0 + TN - 1) / TN);
+        for (uint32_t t = 0; ok && t < ntiles; ++t, ++tcount) {
+          const uint32_t b = tcount & 1u, tph = (tcount >> 1) & 1u;
+          if (!mbar_wait(smem_addr(&bar_tempty[b]), tph ^ 1u, abort_flag, a.err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d_tmem = tmem_base + b * TN;
+          for (uint32_t step = 0; step < steps; ++step) {
+            if (!mbar_wait(smem_addr(&bar_full[s]), ph, abort_flag, a.err)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t st = sbase + s * stage_bytes;
+            const uint64_t dq = sw128_desc(st), dx = sw128_desc(st + PART);
+#pragma unroll
+            for (uint32_t j = 0; j < TKB / 16; ++j) {  // K = 16 per MMA: 32 bytes further along the row
+              const uint64_t o = (uint64_t)(2 * j);
+              umma_bf16(d_tmem, dq + o, dx + o, (step | j) != 0 ? 1u : 0u);
+            }
+            mma_issued = true;
+            umma_commit(smem_addr(&bar_empty[s]));  // frees the stage when these MMAs have read it
+            if (++s == a.stages) {
+              s = 0;
+              ph ^= 1u;
+            }
+          }
+          if (!ok) break;
+          umma_commit(smem_addr(&bar_tfull[b]));  // accumulator b holds tile t
+        }
+      }
+    }
+  } else {
+    // ---------------------------------------------------------------- screening (warps 2-5)
+    const uint32_t quad = warp & 3u;          // TMEM lanes 32 * quad .. + 31
+    const uint32_t et = quad * 32 + lane;     // this thread's query within the tile
+    uint64_t* list = reinterpret_cast<uint64_t*>(smem + a.o_list);
+    uint64_t* buf = reinterpret_cast<uint64_t*>(smem + a.o_buf);
+    uint32_t tcount = 0;
+    bool ok = true;
+    for (uint32_t w = blockIdx.x; ok && w < items; w += gridDim.x) {
+      const uint32_t chunk = w / a.qtiles, qt = w % a.qtiles;
+      const uint64_t r0 = (uint64_t)chunk * a.chunk, r1 = min(a.n, r0 + a.chunk);
+      const uint32_t ntiles = (uint32_t)((r1 - r0 + TN - 1) / TN);
+      const uint32_t q = qt * TM + et;
+      const bool qvalid = q < a.nq;
+      const float qn = qvalid ? a.qnorm[q] : 0.f;
+      const uint64_t self = a.exclude_self ? a.first_row + q : ~0ull;
+      uint32_t lcnt = 0, bcnt = 0;
+      float thr = qvalid ? INFINITY : -1.f;  // a thread past the queries accepts nothing
+      for (uint32_t t = 0; t < ntiles; ++t, ++tcount) {
+        const uint32_t b = tcount & 1u, tph = (tcount >> 1) & 1u;
+        // every lane waits; the vote keeps the warp together for the warp-wide TMEM loads
+        ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&bar_tfull[b]), tph, abort_flag, a.err));
+        if (!ok) break;
+        tc_fence_after();
+        const uint64_t row0 = r0 + (uint64_t)t * TN;
+        const bool edge = row0 + TN > r1 || (self >= row0 && self < row0 + TN);
+        const uint32_t taddr = tmem_base + ((quad * 32u) << 16) + b * TN;
+        const float4* xn4 = reinterpret_cast<const float4*>(a.xnorm + row0);
+#pragma unroll 1
+        for (uint32_t g = 0; g < TN / 32; ++g) {
+          uint32_t v[32];
+          tmem_ld32(taddr + g * 32, v);
+#pragma unroll
+          for (uint32_t h = 0; h < 2; ++h) {
+#pragma unroll
+            for (uint32_t j4 = 0; j4 < 4; ++j4) {
+              const float4 xn = __ldg(xn4 + g * 8 + h * 4 + j4);
+              const float xs[4] = {xn.x, xn.y, xn.z, xn.w};
+#pragma unroll
+              for (uint32_t e = 0; e < 4; ++e) {
+                const uint32_t c = g * 32 + h * 16 + j4 * 4 + e;
+                const float d = fmaxf(fmaf(-2.f, __uint_as_float(v[h * 16 + j4 * 4 + e]), xs[e]) + qn, 0.f);
+                if (d <= thr) {
+                  const uint64_t row = row0 + c;
+                  if (!edge || (row < r1 && row != self)) {
+                    buf[bcnt * TM + et] = ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)row;
+                    ++bcnt;
+                  }
+                }
+              }
+            }
+            if (__any_sync(0xffffffffu, bcnt > BUF - 16)) merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(smem_addr(&bar_tempty[b]));  // accumulator b may be overwritten
+      }
+      if (!ok) break;
+      merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
+      if (qvalid) {
+        uint64_t* dst = a.part + ((uint64_t)q * a.nchunks + chunk) * a.K2;
+        for (uint32_t i = 0; i < a.K2; ++i) dst[i] = i < lcnt ? list[i * TM + et] : ~0ull;
+      }
+    }
+  }
+
+  // ------------------------------------------------------------------------------ teardown
+  __syncthreads();
+  if (warp == 1) {
+    if (lane == 0 && mma_issued) {  // every MMA this thread issued has finished before TMEM is freed
+      umma_commit(smem_addr(&bar_drain));
+      unsigned long long t0 = clock64();
+      while (!mbar_try_wait(smem_addr(&bar_drain), 0)) {
+        if (clock64() - t0 > WAIT_CYCLES) {
+          atomicOr(a.err, 2);
+          break;
+        }
+      }
+    }
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// FP32 rows -> BF16 hi (and lo = x - hi) rows of W values (zero padded), FP32 squared norms (+inf
+// for the padding rows up to norm_rows), and a flag set when some lo is not zero.  A warp per row.
+__global__ void to_bf16_kernel(const float* __restrict__ src, uint64_t rows, uint32_t dim, uint64_t ld, uint32_t W,
+                               __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                               float* __restrict__ norms, uint64_t norm_rows, int* __restrict__ inexact) {
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < norm_rows; r += nw) {
+    if (r >= rows) {
+      if (lane == 0) norms[r] = INFINITY;
+      continue;
+    }
+    float acc = 0.f;
+    bool any_lo = false;
+    for (uint32_t c = lane; c < W; c += 32) {
+      const float x = c < dim ? src[r * ld + c] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+      hi[r * W + c] = h;
+      lo[r * W + c] = l;
+      any_lo |= __bfloat162float(l) != 0.f;
+      acc = fmaf(x, x, acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) norms[r] = acc;
+    if (__any_sync(0xffffffffu, any_lo) && lane == 0) atomicOr(inexact, 1);
+  }
+}
+
+// cuTensorMapEncodeTiled from the driver, found once through the runtime (no link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Tensor map of `rows` BF16 rows of W values (W a multiple of 64): boxes of 64 values x 128 rows,
+// 128-byte swizzle; rows past the end read as zeros.
+int make_map(CUtensorMap* m, const __nv_bfloat16* p, uint64_t rows, uint32_t W) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return fail(EFG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  cuuint64_t dims[2] = {W, rows};
+  cuuint64_t strides[1] = {(cuuint64_t)W * 2};
+  cuuint32_t box[2] = {TKB, TM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(p), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(EFG_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return EFG_OK;
+}
+
+}  // namespace
+
+// Largest k the tensor-core path serves (the per-thread lists of K2 = k + 16 keys and the buffers
+// must fit in shared memory beside two pipeline stages of the split form).
+uint32_t tc_knn_max_k() { return 104; }
+
+int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                       uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                       cudaStream_t s, int force_split) {
+  if (nq == 0) return EFG_OK;
+  if (n >= (1ull << 31) || nq >= (1ull << 31)) return fail(EFG_ERR_ARG, "tensor-core k-NN: more than 2^31 rows");
+  if (k > tc_knn_max_k()) return fail(EFG_ERR_ARG, "tensor-core k-NN: k above " + std::to_string(tc_knn_max_k()));
+  const uint32_t K2 = (uint32_t)std::min<uint64_t>(k + 16, n);
+  const uint32_t W = (dim + TKB - 1) / TKB * TKB;
+  const uint32_t kblocks = W / TKB;
+  const uint64_t qtiles = (nq + TM - 1) / TM;
+  const uint64_t nrows_pad = (n + TN - 1) / TN * TN;
+
+  int dev = 0, sms = 148;
+  EFG_CUDA(cudaGetDevice(&dev));
+  EFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int smem_max = 0;
+  EFG_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+
+  // operands: BF16 hi/lo rows, norms, the inexact flag and the error word
+  __nv_bfloat16 *xh = nullptr, *xl = nullptr, *qh = nullptr, *ql = nullptr;
+  float *xn = nullptr, *qn = nullptr;
+  int* flags = nullptr;
+  uint64_t* part = nullptr;
+  auto release = [&] {
+    cudaFreeAsync(xh, s);
+    cudaFreeAsync(xl, s);
+    cudaFreeAsync(qh, s);
+    cudaFreeAsync(ql, s);
+    cudaFreeAsync(xn, s);
+    cudaFreeAsync(qn, s);
+    cudaFreeAsync(flags, s);
+    cudaFreeAsync(part, s);
+  };
+  struct Guard {
+    decltype(release)& f;
+    ~Guard() { f(); }
+  } guard{release};
+  EFG_CUDA(cudaMallocAsync((void**)&xh, n * W * 2, s));
+  EFG_CUDA(cudaMallocAsync((void**)&xl, n * W * 2, s));
+  EFG_CUDA(cudaMallocAsync((void**)&qh, nq * W * 2, s));
+  EFG_CUDA(cudaMallocAsync((void**)&ql, nq * W * 2, s));
+  EFG_CUDA(cudaMallocAsync((void**)&xn, nrows_pad * 4, s));
+  EFG_CUDA(cudaMallocAsync((void**)&qn, nq * 4, s));
+  EFG_CUDA(cudaMallocAsync((void**)&flags, 8, s));
+  EFG_CUDA(cudaMemsetAsync(flags, 0, 8, s));
+  {
+    const uint64_t warps = std::min<uint64_t>(nrows_pad, (uint64_t)sms * 64);
+    to_bf16_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(base, n, dim, ld, W, xh, xl, xn, nrows_pad,
+                                                                        flags);
+    EFG_CUDA(cudaGetLastError());
+    const uint64_t qwarps = std::min<uint64_t>(nq, (uint64_t)sms * 64);
+    to_bf16_kernel<<<(unsigned)((qwarps * 32 + 255) / 256), 256, 0, s>>>(q, nq, dim, qld, W, qh, ql, qn, nq, flags);
+    EFG_CUDA(cudaGetLastError());
+  }
+  int hflags[2] = {0, 0};
+  EFG_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, s));
+  EFG_CUDA(cudaStreamSynchronize(s));
+  const uint32_t terms = (hflags[0] || force_split) ? 3u : 1u;
+
+  // shared memory: pipeline stages, then the per-thread lists and buffers
+  const uint32_t stage_bytes = 2 * PART;
+  const uint32_t epi = TM * (K2 + BUF) * 8;
+  const int64_t room = (int64_t)smem_max - 1024 - 2048 - epi;  // alignment pad, static barriers
+  const uint32_t stages = (uint32_t)std::min<int64_t>(MAX_STAGES, std::max<int64_t>(0, room / stage_bytes));
+  if (stages < 2) return fail(EFG_ERR_ARG, "tensor-core k-NN: k too large for shared memory");
+  const uint32_t o_list = stages * stage_bytes, o_buf = o_list + TM * K2 * 8;
+  const size_t smem = 1024 + (size_t)o_buf + TM * BUF * 8;
+
+  // work items: (query tile, base chunk); about 8 per SM, balanced over the SMs
+  uint64_t best_nc = 1;
+  double best_cost = 1e300;
+  const uint64_t max_nc = std::max<uint64_t>(1, std::min<uint64_t>(4096 / K2, (n + TN - 1) / TN));
+  const uint64_t target = std::max<uint64_t>(1, ((uint64_t)sms * 8 + qtiles - 1) / qtiles);
+  for (uint64_t nc = std::max<uint64_t>(1, target / 2); nc <= std::min(max_nc, target * 2); ++nc) {
+    const uint64_t chunk = ((n + nc - 1) / nc + TN - 1) / TN * TN;
+    const uint64_t real = (n + chunk - 1) / chunk, itm = qtiles * real;
+    const uint64_t waves = (itm + sms - 1) / sms;
+    // time ~ waves x tiles per item; a small merge cost per chunk
+    const double cost = (double)waves * (double)(chunk / TN) + 0.02 * (double)real * (double)(chunk / TN);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best_nc = real;
+    }
+  }
+  const uint64_t chunk = ((n + best_nc - 1) / best_nc + TN - 1) / TN * TN;
+  const uint32_t nchunks = (uint32_t)((n + chunk - 1) / chunk);
+  EFG_CUDA(cudaMallocAsync((void**)&part, nq * nchunks * K2 * 8, s));
+
+  CUtensorMap mqh, mql, mxh, mxl;
+  EFG_TRY(make_map(&mqh, qh, nq, W));
+  EFG_TRY(make_map(&mql, ql, nq, W));
+  EFG_TRY(make_map(&mxh, xh, n, W));
+  EFG_TRY(make_map(&mxl, xl, n, W));
+
+  TcArgs a;
+  a.qnorm = qn;
+  a.xnorm = xn;
+  a.part = part;
+  a.err = flags + 1;
+  a.n = n;
+  a.chunk = chunk;
+  a.first_row = first_row;
+  a.nq = (uint32_t)nq;
+  a.qtiles = (uint32_t)qtiles;
+  a.nchunks = nchunks;
+  a.K2 = K2;
+  a.kblocks = kblocks;
+  a.terms = terms;
+  a.stages = stages;
+  a.exclude_self = exclude_self ? 1u : 0u;
+  a.o_list = o_list;
+  a.o_buf = o_buf;
+  EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const uint64_t items = qtiles * nchunks;
+  const unsigned grid = (unsigned)std::min<uint64_t>(items, (uint64_t)sms);
+  tc_knn_kernel<<<grid, THREADS, smem, s>>>(mqh, mql, mxh, mxl, a);
+  EFG_CUDA(cudaGetLastError());
+  EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks, part, ids, dists, s));
+  EFG_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, s));
+  EFG_CUDA(cudaStreamSynchronize(s));
+  if (hflags[1]) return fail(EFG_ERR_DEVICE_LIMIT, "tensor-core k-NN: a pipeline wait ran out (error word " +
+                                                        std::to_string(hflags[1]) + ")");
+  return EFG_OK;
+}
+
+}  // namespace efg

@@ -242,6 +242,25 @@ static int download_graph(const efg_index* idx, std::vector<uint64_t>& ptr, std:
 
 using namespace efg;
 
+// Argument checks shared by the exact k-NN entry points.
+namespace efg {
+int bf_check_args(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q, uint64_t nq,
+                  uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row, const int32_t* d_ids) {
+  if (!d_base || (!d_q && nq) || (!d_ids && nq)) return fail(EFG_ERR_ARG, "null argument");
+  if (k == 0 || k > 256) return fail(EFG_ERR_ARG, "k must be in [1, 256]");
+  if ((uint64_t)k + (exclude_self ? 1 : 0) > n) return fail(EFG_ERR_ARG, "k larger than the base");
+  if (n > (uint64_t)INT32_MAX) return fail(EFG_ERR_ARG, "base larger than 2^31 - 1 rows (ids are int32)");
+  if (exclude_self && (first_row > n || nq > n - first_row))
+    return fail(EFG_ERR_ARG, "exclude_self: queries first_row .. first_row + nq must be base rows");
+  if (dim == 0) return fail(EFG_ERR_ARG, "dim must be positive");
+  if (row_stride < dim || q_stride < dim || (row_stride % 4) || (q_stride % 4) || (((uintptr_t)d_base) & 15) ||
+      (((uintptr_t)d_q) & 15))
+    return fail(EFG_ERR_ARG, "rows must be 16-byte aligned: strides a multiple of 4 floats");
+  return EFG_OK;
+}
+
+}  // namespace efg
+
 extern "C" {
 
 const char* efg_last_error(void) { return g_last_error.c_str(); }
@@ -638,14 +657,26 @@ int efg_l2_pairs(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_str
 int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
                         uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
                         int32_t* d_ids, float* d_dists, void* stream) {
-  if (!d_base || (!d_q && nq) || (!d_ids && nq)) return fail(EFG_ERR_ARG, "null argument");
-  if (k == 0 || k > 256) return fail(EFG_ERR_ARG, "k must be in [1, 256]");
-  if ((uint64_t)k + (exclude_self ? 1 : 0) > n) return fail(EFG_ERR_ARG, "k larger than the base");
-  if (row_stride < dim || q_stride < dim || (row_stride % 4) || (q_stride % 4) || (((uintptr_t)d_base) & 15) ||
-      (((uintptr_t)d_q) & 15))
-    return fail(EFG_ERR_ARG, "rows must be 16-byte aligned: strides a multiple of 4 floats");
+  EFG_TRY(efg::bf_check_args(d_base, n, dim, row_stride, d_q, nq, q_stride, k, exclude_self, first_row, d_ids));
+  return exact_knn(d_base, n, dim, (uint32_t)row_stride, d_q, nq, (uint32_t)q_stride, k, exclude_self, first_row,
+                   d_ids, d_dists, (cudaStream_t)stream);
+}
+
+int efg_brute_force_knn_fp32(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
+                             uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
+                             int32_t* d_ids, float* d_dists, void* stream) {
+  EFG_TRY(efg::bf_check_args(d_base, n, dim, row_stride, d_q, nq, q_stride, k, exclude_self, first_row, d_ids));
   return brute_force_knn(d_base, n, dim, (uint32_t)row_stride, d_q, nq, (uint32_t)q_stride, k, exclude_self,
                          first_row, d_ids, d_dists, (cudaStream_t)stream);
+}
+
+int efg_brute_force_knn_split(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
+                              uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
+                              int32_t* d_ids, float* d_dists, void* stream) {
+  EFG_TRY(efg::bf_check_args(d_base, n, dim, row_stride, d_q, nq, q_stride, k, exclude_self, first_row, d_ids));
+  if (k > tc_knn_max_k()) return fail(EFG_ERR_ARG, "k above the tensor-core path's limit");
+  return brute_force_knn_tc(d_base, n, dim, (uint32_t)row_stride, d_q, nq, (uint32_t)q_stride, k, exclude_self,
+                            first_row, d_ids, d_dists, (cudaStream_t)stream, 1);
 }
 
 int efg_nnd_init(efg_index* idx, efg_nnd_host_state* st) {

@@ -158,6 +158,23 @@ int launch_l2_pairs(const float* base, uint32_t dim, uint32_t ld, const uint32_t
 int brute_force_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
                     uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
                     cudaStream_t s);
+// index.cu: argument checks of the exact k-NN entry points (null pointers, k, sizes, alignment).
+int bf_check_args(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q, uint64_t nq,
+                  uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row, const int32_t* d_ids);
+// gram_tc.cu: the same results with the screening on the tensor cores (k <= tc_knn_max_k());
+// force_split uses the hi + lo BF16 products even when BF16 holds the data exactly.
+uint32_t tc_knn_max_k();
+int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                       uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                       cudaStream_t s, int force_split = 0);
+// The exact k-NN of the library: tensor-core screening where k allows, else the FP32 kernels.
+inline int exact_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
+                     uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
+                     cudaStream_t s) {
+  if (k <= tc_knn_max_k())
+    return brute_force_knn_tc(base, n, dim, ld, q, nq, qld, k, exclude_self, first_row, ids, dists, s);
+  return brute_force_knn(base, n, dim, ld, q, nq, qld, k, exclude_self, first_row, ids, dists, s);
+}
 
 // trees.cu: builds `ntrees` canonical trees over the index's base (fills idx->forest).
 int build_forest(efg_index* idx, uint32_t ntrees);

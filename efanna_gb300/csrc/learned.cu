@@ -689,7 +689,7 @@ int efg_learned_train(efg_learned* L, const float* d_q, uint64_t n, uint64_t row
   L->ntrain = n;
   for (uint64_t q0 = 0; q0 < n; q0 += 65536) {
     uint64_t m = std::min<uint64_t>(n - q0, 65536);
-    EFG_TRY(brute_force_knn(idx->d_base, idx->n, dim, ld, L->trainq.p + q0 * ld, m, ld, GT_K, 0, 0, gt.p + q0 * GT_K,
+    EFG_TRY(exact_knn(idx->d_base, idx->n, dim, ld, L->trainq.p + q0 * ld, m, ld, GT_K, 0, 0, gt.p + q0 * GT_K,
                             gtd.p + q0 * GT_K, s));
   }
   trace_clusters_kernel<<<1024, 256, 0, s>>>(gt.p, n, L->assign.p, L->tclusters.p);

@@ -58,13 +58,8 @@ extern "C" int efg_brute_force_knn_noalloc(const float* d_base, uint64_t n, uint
                                            const float* d_q, uint64_t nq, uint64_t q_stride, uint32_t k,
                                            int exclude_self, uint64_t first_row, int32_t* d_ids, float* d_dists,
                                            void* stream) {
-  using efg::fail;
-  if (!d_base || (!d_q && nq) || (!d_ids && nq)) return fail(EFG_ERR_ARG, "null argument");
-  if (k == 0 || k > 256) return fail(EFG_ERR_ARG, "k must be in [1, 256]");
-  if ((uint64_t)k + (exclude_self ? 1 : 0) > n) return fail(EFG_ERR_ARG, "k larger than the base");
-  if (row_stride < dim || q_stride < dim || (row_stride % 4) || (q_stride % 4) || (((uintptr_t)d_base) & 15) ||
-      (((uintptr_t)d_q) & 15))
-    return fail(EFG_ERR_ARG, "rows must be 16-byte aligned: strides a multiple of 4 floats");
+  int rc0 = efg::bf_check_args(d_base, n, dim, row_stride, d_q, nq, q_stride, k, exclude_self, first_row, d_ids);
+  if (rc0 != EFG_OK) return rc0;
   uint64_t* scratch = nullptr;
   int rc = scratch_address(&scratch);
   if (rc != EFG_OK) return rc;

@@ -323,11 +323,28 @@ int efg_l2_pairs(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_str
                  const uint32_t* d_b, uint64_t m, float* d_out, void* stream);
 
 /* Exact k-NN by brute force (Matrix::brute_force_search, general/matrix.hpp:57-68), ordered by
- * (dist, id).  If exclude_self is nonzero, query i is base row (first_row + i) and is skipped.
- * Distances are FP32; candidates within the FP32 error band of the k-th are re-ranked in FP64. */
+ * (dist, id).  If exclude_self is nonzero, query i is base row (first_row + i) and is skipped
+ * (those rows must lie in the base).  n <= 2^31 - 1.  Screening keeps, per query and base chunk,
+ * the k + 16 smallest screened distances; the k + 16 best of those over all chunks are re-computed
+ * in FP64 and the k smallest by (FP64 distance, id) are returned, d_dists (may be NULL) receiving
+ * the FP64 distances rounded to FP32.  For k <= 104 the screening runs on the tensor cores
+ * (tcgen05 BF16 Gram tiles, FP32 accumulation): exact on data BF16 holds exactly (integers up to
+ * 256 in magnitude, as the byte-valued data sets), otherwise split into hi + lo BF16 parts with an
+ * error near 2^-16 of |q.x|.  Larger k screen with the FP32 kernel below.  Ids are exact whenever
+ * the true k nearest are among the k + 16 screened survivors of their chunk -- always on exactly
+ * representable data. */
 int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
                         uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
                         int32_t* d_ids, float* d_dists, void* stream);
+/* The same with the screening in FP32 on CUDA cores (squared differences, any k <= 256). */
+int efg_brute_force_knn_fp32(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
+                             uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
+                             int32_t* d_ids, float* d_dists, void* stream);
+/* The tensor-core path with the hi + lo split forced even on exactly representable data (k <= 104;
+ * the lo parts are then zero and the results equal the plain tensor-core path's). */
+int efg_brute_force_knn_split(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
+                              uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
+                              int32_t* d_ids, float* d_dists, void* stream);
 
 /* efg_brute_force_knn without any device allocation, for callers that must not have a library
  * allocate GPU memory during the call (their device memory is owned by another allocator, or the

@@ -168,6 +168,7 @@ def lib():
         "efg_brute_force_knn": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_brute_force_knn_noalloc": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_brute_force_knn_fp32": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
+        "efg_get_knn_stats": (i32, [vp]),
         "efg_brute_force_knn_split": (i32, [vp, u64, u32, u64, vp, u64, u64, u32, i32, u64, vp, vp, vp]),
         "efg_knn_search_batch": (i32, [vp, f32p, u64, u32, u64, vp, u32, C.POINTER(C.c_int32)]),
         "efg_knn_search_batch_device": (i32, [vp, vp, u64, u64, vp, C.POINTER(QueryParams), vp, vp, vp]),
@@ -609,6 +610,19 @@ def l2_pairs_device(base_ptr: int, n: int, dim: int, row_stride: int, a_ptr: int
                     out_ptr: int, stream: int = 0) -> None:
     _check(lib().efg_l2_pairs(C.c_void_p(base_ptr), n, dim, row_stride, C.c_void_p(a_ptr), C.c_void_p(b_ptr), m,
                               C.c_void_p(out_ptr), C.c_void_p(stream)))
+
+
+class KnnStats(C.Structure):
+    _fields_ = [("convert_ms", C.c_double), ("screen_ms", C.c_double), ("merge_ms", C.c_double),
+                ("screen_flops", C.c_double), ("tile_flops", C.c_double), ("terms", C.c_uint32),
+                ("stages", C.c_uint32), ("nchunks", C.c_uint32), ("ctas", C.c_uint32)]
+
+
+def knn_stats() -> KnnStats:
+    """Timing of this thread's last tensor-core exact k-NN call."""
+    st = KnnStats()
+    _check(lib().efg_get_knn_stats(C.byref(st)))
+    return st
 
 
 def brute_force_knn_device(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int, q_stride: int,

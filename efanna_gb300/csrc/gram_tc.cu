@@ -451,6 +451,8 @@ int make_map(CUtensorMap* m, const __nv_bfloat16* p, uint64_t rows, uint32_t W) 
 
 }  // namespace
 
+thread_local efg_knn_stats g_knn_stats = {};
+
 // Largest k the tensor-core path serves (the per-thread lists of K2 = k + 16 keys and the buffers
 // must fit in shared memory beside two pipeline stages of the split form).
 uint32_t tc_knn_max_k() { return 104; }
@@ -500,6 +502,15 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_CUDA(cudaMallocAsync((void**)&qn, nq * 4, s));
   EFG_CUDA(cudaMallocAsync((void**)&flags, 8, s));
   EFG_CUDA(cudaMemsetAsync(flags, 0, 8, s));
+  cudaEvent_t ev[4];
+  for (auto& e : ev) EFG_CUDA(cudaEventCreate(&e));
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+    }
+  } evguard{ev};
+  EFG_CUDA(cudaEventRecord(ev[0], s));
   {
     const uint64_t warps = std::min<uint64_t>(nrows_pad, (uint64_t)sms * 64);
     to_bf16_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(base, n, dim, ld, W, xh, xl, xn, nrows_pad,
@@ -570,11 +581,25 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint64_t items = qtiles * nchunks;
   const unsigned grid = (unsigned)std::min<uint64_t>(items, (uint64_t)sms);
+  EFG_CUDA(cudaEventRecord(ev[1], s));
   tc_knn_kernel<<<grid, THREADS, smem, s>>>(mqh, mql, mxh, mxl, a);
   EFG_CUDA(cudaGetLastError());
+  EFG_CUDA(cudaEventRecord(ev[2], s));
   EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks, part, ids, dists, s));
+  EFG_CUDA(cudaEventRecord(ev[3], s));
   EFG_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, s));
   EFG_CUDA(cudaStreamSynchronize(s));
+  float ms[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+  g_knn_stats.convert_ms = ms[0];
+  g_knn_stats.screen_ms = ms[1];
+  g_knn_stats.merge_ms = ms[2];
+  g_knn_stats.screen_flops = 2.0 * (double)nq * (double)n * (double)dim;
+  g_knn_stats.tile_flops = 2.0 * (double)(qtiles * TM) * (double)(nchunks * chunk) * (double)W * (double)terms;
+  g_knn_stats.terms = terms;
+  g_knn_stats.stages = stages;
+  g_knn_stats.nchunks = nchunks;
+  g_knn_stats.ctas = grid;
   if (hflags[1]) return fail(EFG_ERR_DEVICE_LIMIT, "tensor-core k-NN: a pipeline wait ran out (error word " +
                                                         std::to_string(hflags[1]) + ")");
   return EFG_OK;

@@ -662,6 +662,12 @@ int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t 
                    d_ids, d_dists, (cudaStream_t)stream);
 }
 
+int efg_get_knn_stats(efg_knn_stats* out) {
+  if (!out) return fail(EFG_ERR_ARG, "null argument");
+  *out = g_knn_stats;
+  return EFG_OK;
+}
+
 int efg_brute_force_knn_fp32(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const float* d_q,
                              uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self, uint64_t first_row,
                              int32_t* d_ids, float* d_dists, void* stream) {

@@ -164,6 +164,7 @@ int bf_check_args(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_st
 // gram_tc.cu: the same results with the screening on the tensor cores (k <= tc_knn_max_k());
 // force_split uses the hi + lo BF16 products even when BF16 holds the data exactly.
 uint32_t tc_knn_max_k();
+extern thread_local efg_knn_stats g_knn_stats;  // the calling thread's last tensor-core k-NN call
 int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
                        uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
                        cudaStream_t s, int force_split = 0);

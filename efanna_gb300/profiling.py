@@ -9,11 +9,17 @@
         the base above the L2 size).  --phase-clocks runs the same searches on the diagnostic
         build of the library (EFG_PHASE_CLOCKS: every CTA of nnexp_kernel reports the SM cycles
         of each phase) and prints each search's phase shares after its line.
+    python -m efanna_gb300.profiling knn [--n N] [--nq Q] [--dim D] [--k K] [--data u8|unit]
+                                         [--screening auto|fp32|split] [--repeat R]
+        times the exact k-NN (tensor-core or FP32 screening) on seeded data: per call the
+        library's event times of the conversion, the screening kernel and the merge, and the
+        screening's TFLOP/s against the measured BF16 peak.
 """
 from __future__ import annotations
 
 import argparse
 import collections
+import ctypes
 import csv
 import os
 import subprocess
@@ -60,6 +66,46 @@ def idx_exact(x, q):
     return out.cpu().numpy()
 
 
+def knn_case(n: int, nq: int, dim: int, k: int, data: str, screening: str, repeat: int) -> None:
+    import json
+    import time
+
+    import torch
+
+    import efanna_gb300 as E
+    from efanna_gb300 import datasets
+    if data == "u8":
+        x = datasets.mixture_u8(n, dim, seed=0)
+        q = datasets.mixture_u8(nq, dim, seed=0, queries=True)
+    else:
+        x = datasets.mixture_unit(n, dim, block=16, seed=0)
+        q = datasets.mixture_unit(nq, dim, block=16, seed=0, queries=True)
+    X, Q = torch.from_numpy(x).cuda(), torch.from_numpy(q).cuda()
+    ids = torch.zeros((nq, k), dtype=torch.int32, device="cuda")
+    peak = None
+    pk = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peak = float(json.load(open(pk))["bf16_tflops"])
+    for r in range(repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E.brute_force_knn_device(X.data_ptr(), n, dim, dim, Q.data_ptr(), nq, dim, k, ids.data_ptr(),
+                                 screening=screening)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) * 1e3
+        if screening == "fp32":
+            print("knn fp32 %d x %d, %d queries, k=%d: wall %.2f ms" % (n, dim, nq, k, wall))
+            continue
+        st = E.knn_stats()
+        tf = st.screen_flops / (st.screen_ms * 1e-3) / 1e12
+        tt = st.tile_flops / (st.screen_ms * 1e-3) / 1e12
+        print("knn %s %d x %d, %d queries, k=%d: convert %.3f ms, screen %.3f ms (%.1f TFLOP/s algorithmic, %.1f "
+              "issued%s), merge %.3f ms, wall %.2f ms; terms %d, stages %d, chunks %d, CTAs %d"
+              % (screening, n, dim, nq, k, st.convert_ms, st.screen_ms, tf, tt,
+                 (", %.3f of measured %.0f" % (tt / peak, peak)) if peak else "", st.merge_ms, wall, st.terms,
+                 st.stages, st.nchunks, st.ctas))
+
+
 def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2,
                 method: int = 0, recall: bool = False) -> None:
     import time
@@ -86,10 +132,13 @@ def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp3
                 wall = time.perf_counter() - t0
                 rec = "" if gt is None else ", recall@10 %.4f" % np.mean(
                     [len(set(r) & set(g)) / 10 for r, g in zip(res, gt)])
+                # the diagnostic build's device printf lines sit in the C library's stdout buffer: push them
+                # out before this search's line so that each search's counters precede its line
+                ctypes.CDLL(None).fflush(None)
                 print("search %s method %d %d/%d/%d, %d queries: %.3f ms kernel (%d launches), %.1f evals/query, "
                       "%.1f expanded/query, %d overflow, wall %.3f s%s" %
                       (prec, method, pt[0], pt[1], pt[2], nq, s.device_ms, s.kernel_launches, s.distance_evals / nq,
-                       s.expanded_nodes / nq, s.overflow_queries, wall, rec))
+                       s.expanded_nodes / nq, s.overflow_queries, wall, rec), flush=True)
 
 
 PHASES = ("setup", "tree descent", "leaf-sequence scan", "pool fill", "pool distances", "pool folds",
@@ -153,8 +202,18 @@ if __name__ == "__main__":
     s.add_argument("--recall", action="store_true", help="also report recall@10 against the exact 10-NN")
     s.add_argument("--phase-clocks", action="store_true",
                    help="run on the diagnostic build and print per-phase cycle shares of nnexp_kernel")
+    kn = sub.add_parser("knn")
+    kn.add_argument("--n", type=int, default=1000000)
+    kn.add_argument("--nq", type=int, default=10000)
+    kn.add_argument("--dim", type=int, default=128)
+    kn.add_argument("--k", type=int, default=10)
+    kn.add_argument("--data", default="u8", choices=["u8", "unit"])
+    kn.add_argument("--screening", default="auto", choices=["auto", "fp32", "split"])
+    kn.add_argument("--repeat", type=int, default=3)
     a = ap.parse_args()
-    if a.cmd == "table":
+    if a.cmd == "knn":
+        knn_case(a.n, a.nq, a.dim, a.k, a.data, a.screening, a.repeat)
+    elif a.cmd == "table":
         print(launch_table(a.csv))
     elif a.cmd == "search" and a.phase_clocks:
         sys.exit(run_phase_clocks(sys.argv[1:]))

@@ -17,8 +17,8 @@ torch = pytest.importorskip("torch")
 
 def _knn(efg, x, q, k, screening, exclude=False, first_row=0, stride=None, qstride=None, stream=0):
     n, d = x.shape
-    ld = stride or d
-    qld = qstride or d
+    ld = stride or (d + 3) // 4 * 4   # rows start on 16-byte boundaries
+    qld = qstride or (d + 3) // 4 * 4
     xp = np.zeros((n, ld), np.float32)
     xp[:, :d] = x
     qp = np.zeros((q.shape[0], qld), np.float32)

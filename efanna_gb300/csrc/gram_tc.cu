@@ -21,9 +21,12 @@
 //     tcgen05.ld, one query per thread, turn each Gram value into a distance and keep the
 //     query's best K2 = k + 16 (distance, id) keys of the chunk.  The two accumulators let the
 //     MMAs of tile t + 1 run while tile t is being screened.
-//   * each thread's candidates first go to a small buffer in shared memory; when any lane's buffer
-//     nears full, the warp merges its buffers into the threads' sorted lists and tightens the
-//     thresholds, so the per-value work is one FMA, one compare and (rarely) one store.
+//   * per group of 64 values a branch-free test (one FMA and one compare per value against the
+//     thread's bound) decides whether any lane of the warp has a candidate; only then does the warp
+//     run the exact per-value test, whose candidates go to a small per-thread buffer in shared
+//     memory, merged into the thread's sorted list (tightening its bound) when any lane's buffer
+//     nears full.  The base-row norms of the next tile are loaded while the current one is
+//     screened, and the second half of the accumulator is read from TMEM during the first.
 //
 // The chunks' lists are the same per-(query, chunk) lists the FP32 kernel writes (distance.cu);
 // the same merge kernel then re-ranks the K2 survivors of each query in FP64.  Every wait on an
@@ -69,7 +72,7 @@ struct TcArgs {
   int* err;
   uint64_t n, chunk, first_row;
   uint32_t nq, qtiles, nchunks, K2, kblocks, terms, stages, exclude_self;
-  uint32_t o_list, o_buf;  // byte offsets of the lists and buffers in dynamic shared memory
+  uint32_t o_list, o_buf, o_xn;  // byte offsets of the lists, buffers and norm copies in dynamic shared memory
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -143,23 +146,23 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// 32 lanes x 32 consecutive FP32 columns (two x16 loads, one wait): thread i of the warp receives
-// the 32 values of TMEM lane (lane base + i) starting at the address's column.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+// 32 lanes x 16 consecutive FP32 columns: thread i of the warp receives the 16 values of TMEM lane
+// (lane base + i) from the address's column on.  Asynchronous until tmem_wait().
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
       "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr + 16));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
+  tmem_ld16(taddr, r);
+  tmem_ld16(taddr + 16, r + 16);
+  tmem_ld16(taddr + 32, r + 32);
+  tmem_ld16(taddr + 48, r + 48);
+}
+__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Merges a thread's buffered keys into its sorted list of at most K2 keys.  Lists and buffers are
 // slot-major with a stride of 128 (the screening threads), so the threads of a warp touch
@@ -303,10 +306,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------------------------------------------------------- screening (warps 2-5)
-    const uint32_t quad = warp & 3u;          // TMEM lanes 32 * quad .. + 31
-    const uint32_t et = quad * 32 + lane;     // this thread's query within the tile
+    const uint32_t quad = warp & 3u;       // TMEM lanes 32 * quad .. + 31
+    const uint32_t et = quad * 32 + lane;  // this thread's query within the tile
     uint64_t* list = reinterpret_cast<uint64_t*>(smem + a.o_list);
     uint64_t* buf = reinterpret_cast<uint64_t*>(smem + a.o_buf);
+    // base-row norms of the current and the next tile, one copy per warp (warp-local hand-over)
+    float* xw = reinterpret_cast<float*>(smem + a.o_xn) + (warp - 2) * 2 * TN;
     uint32_t tcount = 0;
     bool ok = true;
     for (uint32_t w = blockIdx.x; ok && w < items; w += gridDim.x) {
@@ -318,31 +323,54 @@ __global__ void __launch_bounds__(THREADS, 1)
       const float qn = qvalid ? a.qnorm[q] : 0.f;
       const uint64_t self = a.exclude_self ? a.first_row + q : ~0ull;
       uint32_t lcnt = 0, bcnt = 0;
-      float thr = qvalid ? INFINITY : -1.f;  // a thread past the queries accepts nothing
+      float thr = qvalid ? INFINITY : -1.f;  // distance of the K2-th key so far; a thread past the queries accepts nothing
+      // the fast test compares xn - 2 q.x against thr - qn, widened by a few ulps so that it never
+      // rejects what the exact test (d = xn - 2 q.x + qn <= thr) accepts
+      auto bound = [&](float t) { return qvalid ? t - qn + (fabsf(t) + qn) * 4.8e-7f : -INFINITY; };
+      float lim = bound(thr);
+      reinterpret_cast<float4*>(xw + (tcount & 1u) * TN)[lane] =
+          __ldg(reinterpret_cast<const float4*>(a.xnorm + r0) + lane);
+      __syncwarp();
       for (uint32_t t = 0; t < ntiles; ++t, ++tcount) {
         const uint32_t b = tcount & 1u, tph = (tcount >> 1) & 1u;
+        const uint64_t row0 = r0 + (uint64_t)t * TN;
+        const bool more = t + 1 < ntiles;
+        float4 xnext = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (more) xnext = __ldg(reinterpret_cast<const float4*>(a.xnorm + row0 + TN) + lane);  // in flight meanwhile
         // every lane waits; the vote keeps the warp together for the warp-wide TMEM loads
         ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&bar_tfull[b]), tph, abort_flag, a.err));
         if (!ok) break;
         tc_fence_after();
-        const uint64_t row0 = r0 + (uint64_t)t * TN;
         const bool edge = row0 + TN > r1 || (self >= row0 && self < row0 + TN);
         const uint32_t taddr = tmem_base + ((quad * 32u) << 16) + b * TN;
-        const float4* xn4 = reinterpret_cast<const float4*>(a.xnorm + row0);
-#pragma unroll 1
-        for (uint32_t g = 0; g < TN / 32; ++g) {
-          uint32_t v[32];
-          tmem_ld32(taddr + g * 32, v);
+        const float* xs = xw + (tcount & 1u) * TN;
+        uint32_t va[64], vb[64];
+        tmem_ld64(taddr, va);
+        tmem_wait();
+        tmem_ld64(taddr + 64, vb);  // the second half arrives while the first is screened
 #pragma unroll
-          for (uint32_t h = 0; h < 2; ++h) {
+        for (uint32_t half = 0; half < 2; ++half) {
+          if (half == 1) tmem_wait();
+          const uint32_t* v = half == 0 ? va : vb;
+          const float4* x4 = reinterpret_cast<const float4*>(xs + half * 64);
+          // fast path: is any of these 64 values below the thread's bound?
+          bool h0 = false, h1 = false, h2 = false, h3 = false;
 #pragma unroll
-            for (uint32_t j4 = 0; j4 < 4; ++j4) {
-              const float4 xn = __ldg(xn4 + g * 8 + h * 4 + j4);
-              const float xs[4] = {xn.x, xn.y, xn.z, xn.w};
+          for (uint32_t j4 = 0; j4 < 16; ++j4) {
+            const float4 xn = x4[j4];
+            h0 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 0]), xn.x) <= lim;
+            h1 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 1]), xn.y) <= lim;
+            h2 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 2]), xn.z) <= lim;
+            h3 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 3]), xn.w) <= lim;
+          }
+          if (__any_sync(0xffffffffu, h0 | h1 | h2 | h3)) {
+            // slow path (rare once the bounds are tight): the exact test per value, into the buffer
 #pragma unroll
-              for (uint32_t e = 0; e < 4; ++e) {
-                const uint32_t c = g * 32 + h * 16 + j4 * 4 + e;
-                const float d = fmaxf(fmaf(-2.f, __uint_as_float(v[h * 16 + j4 * 4 + e]), xs[e]) + qn, 0.f);
+            for (uint32_t g = 0; g < 4; ++g) {
+#pragma unroll
+              for (uint32_t j = 0; j < 16; ++j) {
+                const uint32_t c = half * 64 + g * 16 + j;
+                const float d = fmaxf(fmaf(-2.f, __uint_as_float(v[g * 16 + j]), xs[c]) + qn, 0.f);
                 if (d <= thr) {
                   const uint64_t row = row0 + c;
                   if (!edge || (row < r1 && row != self)) {
@@ -351,12 +379,17 @@ __global__ void __launch_bounds__(THREADS, 1)
                   }
                 }
               }
+              if (__any_sync(0xffffffffu, bcnt > BUF - 16)) {
+                merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
+                lim = bound(thr);
+              }
             }
-            if (__any_sync(0xffffffffu, bcnt > BUF - 16)) merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
           }
         }
         tc_fence_before();
         mbar_arrive(smem_addr(&bar_tempty[b]));  // accumulator b may be overwritten
+        if (more) reinterpret_cast<float4*>(xw + ((tcount + 1) & 1u) * TN)[lane] = xnext;
+        __syncwarp();
       }
       if (!ok) break;
       merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
@@ -527,12 +560,12 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
 
   // shared memory: pipeline stages, then the per-thread lists and buffers
   const uint32_t stage_bytes = 2 * PART;
-  const uint32_t epi = TM * (K2 + BUF) * 8;
+  const uint32_t epi = TM * (K2 + BUF) * 8 + 4 * 2 * TN * 4;
   const int64_t room = (int64_t)smem_max - 1024 - 2048 - epi;  // alignment pad, static barriers
   const uint32_t stages = (uint32_t)std::min<int64_t>(MAX_STAGES, std::max<int64_t>(0, room / stage_bytes));
   if (stages < 2) return fail(EFG_ERR_ARG, "tensor-core k-NN: k too large for shared memory");
-  const uint32_t o_list = stages * stage_bytes, o_buf = o_list + TM * K2 * 8;
-  const size_t smem = 1024 + (size_t)o_buf + TM * BUF * 8;
+  const uint32_t o_list = stages * stage_bytes, o_buf = o_list + TM * K2 * 8, o_xn = o_buf + TM * BUF * 8;
+  const size_t smem = 1024 + (size_t)o_xn + 4 * 2 * TN * 4;
 
   // work items: (query tile, base chunk); about 8 per SM, balanced over the SMs
   uint64_t best_nc = 1;
@@ -578,6 +611,7 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   a.exclude_self = exclude_self ? 1u : 0u;
   a.o_list = o_list;
   a.o_buf = o_buf;
+  a.o_xn = o_xn;
   EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint64_t items = qtiles * nchunks;
   const unsigned grid = (unsigned)std::min<uint64_t>(items, (uint64_t)sms);

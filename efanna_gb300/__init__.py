@@ -613,9 +613,10 @@ def l2_pairs_device(base_ptr: int, n: int, dim: int, row_stride: int, a_ptr: int
 
 
 class KnnStats(C.Structure):
-    _fields_ = [("convert_ms", C.c_double), ("screen_ms", C.c_double), ("merge_ms", C.c_double),
-                ("screen_flops", C.c_double), ("tile_flops", C.c_double), ("terms", C.c_uint32),
-                ("stages", C.c_uint32), ("nchunks", C.c_uint32), ("ctas", C.c_uint32)]
+    _fields_ = [("convert_ms", C.c_double), ("bound_ms", C.c_double), ("screen_ms", C.c_double),
+                ("merge_ms", C.c_double), ("screen_flops", C.c_double), ("tile_flops", C.c_double),
+                ("terms", C.c_uint32), ("stages", C.c_uint32), ("nchunks", C.c_uint32), ("ctas", C.c_uint32),
+                ("sample_rows", C.c_uint32)]
 
 
 def knn_stats() -> KnnStats:

@@ -21,12 +21,14 @@
 //     tcgen05.ld, one query per thread, turn each Gram value into a distance and keep the
 //     query's best K2 = k + 16 (distance, id) keys of the chunk.  The two accumulators let the
 //     MMAs of tile t + 1 run while tile t is being screened.
-//   * per group of 64 values a branch-free test (one FMA and one compare per value against the
-//     thread's bound) decides whether any lane of the warp has a candidate; only then does the warp
-//     run the exact per-value test, whose candidates go to a small per-thread buffer in shared
-//     memory, merged into the thread's sorted list (tightening its bound) when any lane's buffer
-//     nears full.  The base-row norms of the next tile are loaded while the current one is
-//     screened, and the second half of the accumulator is read from TMEM during the first.
+//   * every query starts with a bound on its K2-th distance: the K2-th distance over a strided
+//     sample of the base, from a first pass of the same kernel over the sample alone (any subset's
+//     K2-th distance bounds the whole base's from above).  Per group of 64 values a branch-free
+//     test (one FMA, one compare per value) builds each thread's mask of values under its bound;
+//     only values in some mask reach the exact test, one per lane per round, and go straight into
+//     the thread's sorted list in shared memory, which tightens the bound once it holds K2 keys.
+//     The base-row norms of the next tile are loaded while the current one is screened, and the
+//     second half of the accumulator is read from TMEM during the first.
 //
 // The chunks' lists are the same per-(query, chunk) lists the FP32 kernel writes (distance.cu);
 // the same merge kernel then re-ranks the K2 survivors of each query in FP64.  Every wait on an
@@ -55,7 +57,7 @@ constexpr uint32_t TM = 128;           // queries per tile (MMA M, TMEM lanes)
 constexpr uint32_t TN = 128;           // base rows per tile (MMA N, TMEM columns per accumulator)
 constexpr uint32_t TKB = 64;           // BF16 values per k-block: one 128-byte swizzle row
 constexpr uint32_t PART = TM * TKB * 2;  // bytes of one 128 x 64 BF16 operand block (16 KiB)
-constexpr uint32_t BUF = 32;           // candidate buffer slots per thread
+constexpr uint32_t SCR = 64;           // per-thread scratch of one group's values (floats)
 constexpr uint32_t THREADS = 192;      // warp 0 TMA, warp 1 MMA (+TMEM), warps 2-5 screening
 constexpr uint32_t MAX_STAGES = 8;
 constexpr uint32_t TMEM_COLS = 2 * TN;  // two FP32 accumulators of 128 columns
@@ -68,11 +70,12 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((TN >> 3) << 17
 struct TcArgs {
   const float* qnorm;  // nq FP32 squared norms
   const float* xnorm;  // squared norms of the base rows, +inf past n (rounded up to a tile)
+  const float* qbound; // per query an upper bound of its K2-th distance, or null (+inf)
   uint64_t* part;      // nq x nchunks x K2 keys
   int* err;
   uint64_t n, chunk, first_row;
   uint32_t nq, qtiles, nchunks, K2, kblocks, terms, stages, exclude_self;
-  uint32_t o_list, o_buf, o_xn;  // byte offsets of the lists, buffers and norm copies in dynamic shared memory
+  uint32_t o_list, o_scr, o_xn;  // byte offsets of the lists, scratch and norm copies in dynamic shared memory
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -164,26 +167,20 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
 }
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Merges a thread's buffered keys into its sorted list of at most K2 keys.  Lists and buffers are
-// slot-major with a stride of 128 (the screening threads), so the threads of a warp touch
-// consecutive words.
-__device__ __forceinline__ void merge_buffer(uint64_t* list, const uint64_t* buf, uint32_t t, uint32_t K2,
-                                             uint32_t& lcnt, uint32_t& bcnt, float& thr) {
-  for (uint32_t i = 0; i < bcnt; ++i) {
-    uint64_t key = buf[i * TM + t];
-    if (lcnt == K2 && key >= list[(K2 - 1) * TM + t]) continue;
-    uint32_t j = lcnt < K2 ? lcnt : K2 - 1;  // a full list drops its last key
-    while (j > 0) {
-      uint64_t prev = list[(j - 1) * TM + t];
-      if (prev <= key) break;
-      list[j * TM + t] = prev;
-      --j;
-    }
-    list[j * TM + t] = key;
-    if (lcnt < K2) ++lcnt;
+// Inserts a key into a thread's sorted list of at most K2 keys (a full list drops its last key).
+// Lists are slot-major with a stride of 128 (the screening threads), so the threads of a warp
+// touch consecutive words.
+__device__ __forceinline__ void insert_key(uint64_t* list, uint32_t t, uint32_t K2, uint32_t& lcnt, uint64_t key) {
+  if (lcnt == K2 && key >= list[(K2 - 1) * TM + t]) return;
+  uint32_t j = lcnt < K2 ? lcnt : K2 - 1;
+  while (j > 0) {
+    const uint64_t prev = list[(j - 1) * TM + t];
+    if (prev <= key) break;
+    list[j * TM + t] = prev;
+    --j;
   }
-  bcnt = 0;
-  if (lcnt == K2) thr = __uint_as_float((uint32_t)(list[(K2 - 1) * TM + t] >> 32));
+  list[j * TM + t] = key;
+  if (lcnt < K2) ++lcnt;
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -309,7 +306,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t quad = warp & 3u;       // TMEM lanes 32 * quad .. + 31
     const uint32_t et = quad * 32 + lane;  // this thread's query within the tile
     uint64_t* list = reinterpret_cast<uint64_t*>(smem + a.o_list);
-    uint64_t* buf = reinterpret_cast<uint64_t*>(smem + a.o_buf);
+    // this thread's copy of a group's 64 values: float4 slot j4 stored at j4 ^ (et & 15), so that the
+    // eight threads of a quarter warp write different banks
+    float* scr = reinterpret_cast<float*>(smem + a.o_scr) + et * SCR;
+    const uint32_t sw = et & 15u;
     // base-row norms of the current and the next tile, one copy per warp (warp-local hand-over)
     float* xw = reinterpret_cast<float*>(smem + a.o_xn) + (warp - 2) * 2 * TN;
     uint32_t tcount = 0;
@@ -322,9 +322,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       const bool qvalid = q < a.nq;
       const float qn = qvalid ? a.qnorm[q] : 0.f;
       const uint64_t self = a.exclude_self ? a.first_row + q : ~0ull;
-      uint32_t lcnt = 0, bcnt = 0;
-      float thr = qvalid ? INFINITY : -1.f;  // distance of the K2-th key so far; a thread past the queries accepts nothing
-      // the fast test compares xn - 2 q.x against thr - qn, widened by a few ulps so that it never
+      uint32_t lcnt = 0;
+      // distance bound: the K2-th key's once the list is full; a thread past the queries accepts nothing
+      float thr = qvalid ? (a.qbound ? a.qbound[q] : INFINITY) : -1.f;
+      // the mask test compares xn - 2 q.x against thr - qn, widened by a few ulps so that it never
       // rejects what the exact test (d = xn - 2 q.x + qn <= thr) accepts
       auto bound = [&](float t) { return qvalid ? t - qn + (fabsf(t) + qn) * 4.8e-7f : -INFINITY; };
       float lim = bound(thr);
@@ -353,35 +354,47 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (half == 1) tmem_wait();
           const uint32_t* v = half == 0 ? va : vb;
           const float4* x4 = reinterpret_cast<const float4*>(xs + half * 64);
-          // fast path: is any of these 64 values below the thread's bound?
-          bool h0 = false, h1 = false, h2 = false, h3 = false;
+          uint32_t m0 = 0, m1 = 0;  // values 0-31 and 32-63 under the bound
 #pragma unroll
           for (uint32_t j4 = 0; j4 < 16; ++j4) {
             const float4 xn = x4[j4];
-            h0 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 0]), xn.x) <= lim;
-            h1 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 1]), xn.y) <= lim;
-            h2 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 2]), xn.z) <= lim;
-            h3 |= fmaf(-2.f, __uint_as_float(v[4 * j4 + 3]), xn.w) <= lim;
+            const uint32_t bits = (fmaf(-2.f, __uint_as_float(v[4 * j4 + 0]), xn.x) <= lim ? 1u : 0u) |
+                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 1]), xn.y) <= lim ? 2u : 0u) |
+                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 2]), xn.z) <= lim ? 4u : 0u) |
+                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 3]), xn.w) <= lim ? 8u : 0u);
+            if (j4 < 8) m0 |= bits << (4 * j4);
+            else m1 |= bits << (4 * (j4 - 8));
           }
-          if (__any_sync(0xffffffffu, h0 | h1 | h2 | h3)) {
-            // slow path (rare once the bounds are tight): the exact test per value, into the buffer
+          if (__any_sync(0xffffffffu, (m0 | m1) != 0u)) {
+            if ((m0 | m1) != 0u) {
 #pragma unroll
-            for (uint32_t g = 0; g < 4; ++g) {
-#pragma unroll
-              for (uint32_t j = 0; j < 16; ++j) {
-                const uint32_t c = half * 64 + g * 16 + j;
-                const float d = fmaxf(fmaf(-2.f, __uint_as_float(v[g * 16 + j]), xs[c]) + qn, 0.f);
-                if (d <= thr) {
-                  const uint64_t row = row0 + c;
-                  if (!edge || (row < r1 && row != self)) {
-                    buf[bcnt * TM + et] = ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)row;
-                    ++bcnt;
+              for (uint32_t j4 = 0; j4 < 16; ++j4)
+                reinterpret_cast<float4*>(scr)[j4 ^ sw] =
+                    make_float4(__uint_as_float(v[4 * j4]), __uint_as_float(v[4 * j4 + 1]),
+                                __uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3]));
+            }
+            // one marked value per lane per round, exact test, straight into the sorted list
+            while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) {
+              if ((m0 | m1) != 0u) {
+                uint32_t j;
+                if (m0) {
+                  j = __ffs(m0) - 1;
+                  m0 &= m0 - 1;
+                } else {
+                  j = 32 + __ffs(m1) - 1;
+                  m1 &= m1 - 1;
+                }
+                const float val = scr[(((j >> 2) ^ sw) << 2) | (j & 3u)];
+                const uint32_t c = half * 64 + j;
+                const float d = fmaxf(fmaf(-2.f, val, xs[c]) + qn, 0.f);
+                const uint64_t row = row0 + c;
+                if (d <= thr && (!edge || (row < r1 && row != self))) {
+                  insert_key(list, et, a.K2, lcnt, ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)row);
+                  if (lcnt == a.K2) {
+                    thr = __uint_as_float((uint32_t)(list[(a.K2 - 1) * TM + et] >> 32));
+                    lim = bound(thr);
                   }
                 }
-              }
-              if (__any_sync(0xffffffffu, bcnt > BUF - 16)) {
-                merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
-                lim = bound(thr);
               }
             }
           }
@@ -392,7 +405,6 @@ __global__ void __launch_bounds__(THREADS, 1)
         __syncwarp();
       }
       if (!ok) break;
-      merge_buffer(list, buf, et, a.K2, lcnt, bcnt, thr);
       if (qvalid) {
         uint64_t* dst = a.part + ((uint64_t)q * a.nchunks + chunk) * a.K2;
         for (uint32_t i = 0; i < a.K2; ++i) dst[i] = i < lcnt ? list[i * TM + et] : ~0ull;
@@ -446,6 +458,34 @@ __global__ void to_bf16_kernel(const float* __restrict__ src, uint64_t rows, uin
     acc = warp_sum(acc);
     if (lane == 0) norms[r] = acc;
     if (__any_sync(0xffffffffu, any_lo) && lane == 0) atomicOr(inexact, 1);
+  }
+}
+
+// Rows floor(i * n / S) of the converted base (hi, lo, norm) into S contiguous sample rows (a warp
+// per row, 16-byte copies; W BF16 values per row).
+__global__ void sample_rows_kernel(const uint4* __restrict__ hi, const uint4* __restrict__ lo,
+                                   const float* __restrict__ norms, uint64_t n, uint32_t W, uint32_t S,
+                                   uint4* __restrict__ shi, uint4* __restrict__ slo, float* __restrict__ snorms) {
+  const uint32_t lane = threadIdx.x & 31, w16 = W / 8;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < S; i += nw) {
+    const uint64_t r = i * n / S;
+    for (uint32_t c = lane; c < w16; c += 32) {
+      shi[i * w16 + c] = hi[r * w16 + c];
+      slo[i * w16 + c] = lo[r * w16 + c];
+    }
+    if (lane == 0) snorms[i] = norms[r];
+  }
+}
+
+// Per query the distance of the rank-th key of its list (nq lists of `stride` keys), widened by
+// `rel` (the split form's two passes may round differently); +inf when the list is shorter.
+__global__ void bound_kernel(const uint64_t* __restrict__ lists, uint64_t nq, uint32_t stride, uint32_t rank,
+                             float rel, float* __restrict__ out) {
+  for (uint64_t qi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = lists[qi * stride + rank - 1];
+    const float d = __uint_as_float((uint32_t)(key >> 32));
+    out[qi] = key == ~0ull ? INFINITY : d + d * rel;
   }
 }
 
@@ -512,8 +552,15 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   __nv_bfloat16 *xh = nullptr, *xl = nullptr, *qh = nullptr, *ql = nullptr;
   float *xn = nullptr, *qn = nullptr;
   int* flags = nullptr;
-  uint64_t* part = nullptr;
+  uint64_t *part = nullptr, *part0 = nullptr;
+  __nv_bfloat16 *sh = nullptr, *sl = nullptr;
+  float *sn = nullptr, *qbound = nullptr;
   auto release = [&] {
+    cudaFreeAsync(sh, s);
+    cudaFreeAsync(sl, s);
+    cudaFreeAsync(sn, s);
+    cudaFreeAsync(qbound, s);
+    cudaFreeAsync(part0, s);
     cudaFreeAsync(xh, s);
     cudaFreeAsync(xl, s);
     cudaFreeAsync(qh, s);
@@ -535,14 +582,15 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_CUDA(cudaMallocAsync((void**)&qn, nq * 4, s));
   EFG_CUDA(cudaMallocAsync((void**)&flags, 8, s));
   EFG_CUDA(cudaMemsetAsync(flags, 0, 8, s));
-  cudaEvent_t ev[4];
-  for (auto& e : ev) EFG_CUDA(cudaEventCreate(&e));
+  cudaEvent_t ev[5] = {};
   struct EvGuard {
     cudaEvent_t* e;
     ~EvGuard() {
-      for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+      for (int i = 0; i < 5; ++i)
+        if (e[i]) cudaEventDestroy(e[i]);
     }
   } evguard{ev};
+  for (auto& e : ev) EFG_CUDA(cudaEventCreate(&e));
   EFG_CUDA(cudaEventRecord(ev[0], s));
   {
     const uint64_t warps = std::min<uint64_t>(nrows_pad, (uint64_t)sms * 64);
@@ -558,16 +606,93 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_CUDA(cudaStreamSynchronize(s));
   const uint32_t terms = (hflags[0] || force_split) ? 3u : 1u;
 
-  // shared memory: pipeline stages, then the per-thread lists and buffers
+  // shared memory: pipeline stages, then the per-thread lists, scratch and norm copies
   const uint32_t stage_bytes = 2 * PART;
-  const uint32_t epi = TM * (K2 + BUF) * 8 + 4 * 2 * TN * 4;
-  const int64_t room = (int64_t)smem_max - 1024 - 2048 - epi;  // alignment pad, static barriers
-  const uint32_t stages = (uint32_t)std::min<int64_t>(MAX_STAGES, std::max<int64_t>(0, room / stage_bytes));
-  if (stages < 2) return fail(EFG_ERR_ARG, "tensor-core k-NN: k too large for shared memory");
-  const uint32_t o_list = stages * stage_bytes, o_buf = o_list + TM * K2 * 8, o_xn = o_buf + TM * BUF * 8;
-  const size_t smem = 1024 + (size_t)o_xn + 4 * 2 * TN * 4;
+  auto layout = [&](uint32_t K2l, uint32_t& stages, uint32_t& o_list, uint32_t& o_scr, uint32_t& o_xn,
+                    size_t& smem) -> bool {
+    const uint32_t epi = TM * K2l * 8 + TM * SCR * 4 + 4 * 2 * TN * 4;
+    const int64_t room = (int64_t)smem_max - 1024 - 2048 - epi;  // alignment pad, static barriers
+    stages = (uint32_t)std::min<int64_t>(MAX_STAGES, std::max<int64_t>(0, room / stage_bytes));
+    o_list = stages * stage_bytes;
+    o_scr = o_list + TM * K2l * 8;
+    o_xn = o_scr + TM * SCR * 4;
+    smem = 1024 + (size_t)o_xn + 4 * 2 * TN * 4;
+    return stages >= 2;
+  };
+  auto launch = [&](const CUtensorMap& mq_h, const CUtensorMap& mq_l, const CUtensorMap& mx_h,
+                    const CUtensorMap& mx_l, const float* xnorm, uint64_t rows, uint64_t chunk_rows,
+                    uint32_t nch, uint32_t K2l, const float* qb, uint64_t* out, int excl, unsigned* grid_out) -> int {
+    TcArgs a;
+    uint32_t stages, o_list, o_scr, o_xn;
+    size_t smem;
+    if (!layout(K2l, stages, o_list, o_scr, o_xn, smem))
+      return fail(EFG_ERR_ARG, "tensor-core k-NN: k too large for shared memory");
+    a.qnorm = qn;
+    a.xnorm = xnorm;
+    a.qbound = qb;
+    a.part = out;
+    a.err = flags + 1;
+    a.n = rows;
+    a.chunk = chunk_rows;
+    a.first_row = first_row;
+    a.nq = (uint32_t)nq;
+    a.qtiles = (uint32_t)qtiles;
+    a.nchunks = nch;
+    a.K2 = K2l;
+    a.kblocks = kblocks;
+    a.terms = terms;
+    a.stages = stages;
+    a.exclude_self = excl ? 1u : 0u;
+    a.o_list = o_list;
+    a.o_scr = o_scr;
+    a.o_xn = o_xn;
+    EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)std::min<uint64_t>(qtiles * nch, (uint64_t)sms);
+    tc_knn_kernel<<<grid, THREADS, smem, s>>>(mq_h, mq_l, mx_h, mx_l, a);
+    EFG_CUDA(cudaGetLastError());
+    if (grid_out) *grid_out = grid;
+    g_knn_stats.stages = stages;
+    return EFG_OK;
+  };
+  {
+    uint32_t st, o1, o2, o3;
+    size_t sm;
+    if (!layout(K2 + 1, st, o1, o2, o3, sm)) return fail(EFG_ERR_ARG, "tensor-core k-NN: k too large for shared memory");
+  }
 
-  // work items: (query tile, base chunk); about 8 per SM, balanced over the SMs
+  CUtensorMap mqh, mql, mxh, mxl;
+  EFG_TRY(make_map(&mqh, qh, nq, W));
+  EFG_TRY(make_map(&mql, ql, nq, W));
+  EFG_TRY(make_map(&mxh, xh, n, W));
+  EFG_TRY(make_map(&mxl, xl, n, W));
+
+  // 1. bound pass over a strided sample of S base rows: the rank-th distance of the sample, rank =
+  // K2 (+ 1 with exclude_self: the sample may hold the query itself)
+  EFG_CUDA(cudaEventRecord(ev[1], s));
+  uint32_t S = (uint32_t)std::min<uint64_t>(65536, n / 16) / TN * TN;
+  const uint32_t rank = K2 + (exclude_self ? 1u : 0u);
+  if (S >= 4096 && S >= rank) {
+    EFG_CUDA(cudaMallocAsync((void**)&sh, (uint64_t)S * W * 2, s));
+    EFG_CUDA(cudaMallocAsync((void**)&sl, (uint64_t)S * W * 2, s));
+    EFG_CUDA(cudaMallocAsync((void**)&sn, (uint64_t)S * 4, s));
+    EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
+    EFG_CUDA(cudaMallocAsync((void**)&part0, nq * rank * 8, s));
+    sample_rows_kernel<<<(unsigned)std::min<uint64_t>((S + 7) / 8, (uint64_t)sms * 8), 256, 0, s>>>(
+        reinterpret_cast<const uint4*>(xh), reinterpret_cast<const uint4*>(xl), xn, n, W, S,
+        reinterpret_cast<uint4*>(sh), reinterpret_cast<uint4*>(sl), sn);
+    EFG_CUDA(cudaGetLastError());
+    CUtensorMap msh, msl;
+    EFG_TRY(make_map(&msh, sh, S, W));
+    EFG_TRY(make_map(&msl, sl, S, W));
+    EFG_TRY(launch(mqh, mql, msh, msl, sn, S, S, 1, rank, nullptr, part0, 0, nullptr));
+    bound_kernel<<<(unsigned)std::min<uint64_t>((nq + 255) / 256, 4096), 256, 0, s>>>(
+        part0, nq, rank, rank, terms == 1 ? 0.f : 1e-5f, qbound);
+    EFG_CUDA(cudaGetLastError());
+  } else {
+    S = 0;
+  }
+
+  // 2. the whole base in (query tile, base chunk) items, about 8 per SM, balanced over the SMs
   uint64_t best_nc = 1;
   double best_cost = 1e300;
   const uint64_t max_nc = std::max<uint64_t>(1, std::min<uint64_t>(4096 / K2, (n + TN - 1) / TN));
@@ -586,52 +711,24 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   const uint64_t chunk = ((n + best_nc - 1) / best_nc + TN - 1) / TN * TN;
   const uint32_t nchunks = (uint32_t)((n + chunk - 1) / chunk);
   EFG_CUDA(cudaMallocAsync((void**)&part, nq * nchunks * K2 * 8, s));
-
-  CUtensorMap mqh, mql, mxh, mxl;
-  EFG_TRY(make_map(&mqh, qh, nq, W));
-  EFG_TRY(make_map(&mql, ql, nq, W));
-  EFG_TRY(make_map(&mxh, xh, n, W));
-  EFG_TRY(make_map(&mxl, xl, n, W));
-
-  TcArgs a;
-  a.qnorm = qn;
-  a.xnorm = xn;
-  a.part = part;
-  a.err = flags + 1;
-  a.n = n;
-  a.chunk = chunk;
-  a.first_row = first_row;
-  a.nq = (uint32_t)nq;
-  a.qtiles = (uint32_t)qtiles;
-  a.nchunks = nchunks;
-  a.K2 = K2;
-  a.kblocks = kblocks;
-  a.terms = terms;
-  a.stages = stages;
-  a.exclude_self = exclude_self ? 1u : 0u;
-  a.o_list = o_list;
-  a.o_buf = o_buf;
-  a.o_xn = o_xn;
-  EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const uint64_t items = qtiles * nchunks;
-  const unsigned grid = (unsigned)std::min<uint64_t>(items, (uint64_t)sms);
-  EFG_CUDA(cudaEventRecord(ev[1], s));
-  tc_knn_kernel<<<grid, THREADS, smem, s>>>(mqh, mql, mxh, mxl, a);
-  EFG_CUDA(cudaGetLastError());
   EFG_CUDA(cudaEventRecord(ev[2], s));
-  EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks, part, ids, dists, s));
+  unsigned grid = 0;
+  EFG_TRY(launch(mqh, mql, mxh, mxl, xn, n, chunk, nchunks, K2, S ? qbound : nullptr, part, exclude_self, &grid));
   EFG_CUDA(cudaEventRecord(ev[3], s));
+  EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks, part, ids, dists, s));
+  EFG_CUDA(cudaEventRecord(ev[4], s));
   EFG_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, s));
   EFG_CUDA(cudaStreamSynchronize(s));
-  float ms[3] = {0, 0, 0};
-  for (int i = 0; i < 3; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+  float ms[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
   g_knn_stats.convert_ms = ms[0];
-  g_knn_stats.screen_ms = ms[1];
-  g_knn_stats.merge_ms = ms[2];
+  g_knn_stats.bound_ms = ms[1];
+  g_knn_stats.screen_ms = ms[2];
+  g_knn_stats.merge_ms = ms[3];
+  g_knn_stats.sample_rows = S;
   g_knn_stats.screen_flops = 2.0 * (double)nq * (double)n * (double)dim;
   g_knn_stats.tile_flops = 2.0 * (double)(qtiles * TM) * (double)(nchunks * chunk) * (double)W * (double)terms;
   g_knn_stats.terms = terms;
-  g_knn_stats.stages = stages;
   g_knn_stats.nchunks = nchunks;
   g_knn_stats.ctas = grid;
   if (hflags[1]) return fail(EFG_ERR_DEVICE_LIMIT, "tensor-core k-NN: a pipeline wait ran out (error word " +

@@ -339,12 +339,14 @@ int efg_brute_force_knn(const float* d_base, uint64_t n, uint32_t dim, uint64_t 
 /* Timing of this thread's last tensor-core k-NN call (CUDA events on the call's stream). */
 typedef struct efg_knn_stats {
   double convert_ms;    /* BF16 hi/lo rows and FP32 norms of base and queries                       */
+  double bound_ms;      /* the per-query distance bounds from a strided sample of the base          */
   double screen_ms;     /* the tcgen05 screening kernel                                             */
   double merge_ms;      /* per-query merge of the chunk lists and FP64 re-rank                      */
   double screen_flops;  /* algorithmic: 2 x queries x base rows x dim (one Gram contraction)          */
   double tile_flops;    /* issued by the MMAs: whole tiles, 64-value k-blocks, x products per value  */
   uint32_t terms;       /* BF16 products per value: 1 (exact data) or 3 (hi.hi + hi.lo + lo.hi)      */
   uint32_t stages, nchunks, ctas;
+  uint32_t sample_rows; /* base rows of the bound pass (0: none, small bases)                        */
 } efg_knn_stats;
 int efg_get_knn_stats(efg_knn_stats* out);
 /* The same with the screening in FP32 on CUDA cores (squared differences, any k <= 256). */

@@ -99,9 +99,10 @@ def knn_case(n: int, nq: int, dim: int, k: int, data: str, screening: str, repea
         st = E.knn_stats()
         tf = st.screen_flops / (st.screen_ms * 1e-3) / 1e12
         tt = st.tile_flops / (st.screen_ms * 1e-3) / 1e12
-        print("knn %s %d x %d, %d queries, k=%d: convert %.3f ms, screen %.3f ms (%.1f TFLOP/s algorithmic, %.1f "
-              "issued%s), merge %.3f ms, wall %.2f ms; terms %d, stages %d, chunks %d, CTAs %d"
-              % (screening, n, dim, nq, k, st.convert_ms, st.screen_ms, tf, tt,
+        print("knn %s %d x %d, %d queries, k=%d: convert %.3f ms, bound %.3f ms (%d sample rows), screen %.3f ms "
+              "(%.1f TFLOP/s algorithmic, %.1f issued%s), merge %.3f ms, wall %.2f ms; terms %d, stages %d, "
+              "chunks %d, CTAs %d"
+              % (screening, n, dim, nq, k, st.convert_ms, st.bound_ms, st.sample_rows, st.screen_ms, tf, tt,
                  (", %.3f of measured %.0f" % (tt / peak, peak)) if peak else "", st.merge_ms, wall, st.terms,
                  st.stages, st.nchunks, st.ctas))
 

@@ -57,8 +57,11 @@ constexpr uint32_t TM = 128;           // queries per tile (MMA M, TMEM lanes)
 constexpr uint32_t TN = 128;           // base rows per tile (MMA N, TMEM columns per accumulator)
 constexpr uint32_t TKB = 64;           // BF16 values per k-block: one 128-byte swizzle row
 constexpr uint32_t PART = TM * TKB * 2;  // bytes of one 128 x 64 BF16 operand block (16 KiB)
-constexpr uint32_t SCR = 64;           // per-thread scratch of one group's values (floats)
-constexpr uint32_t THREADS = 192;      // warp 0 TMA, warp 1 MMA (+TMEM), warps 2-5 screening
+constexpr uint32_t GRP = 16;           // values per screening group (one any-hit vote)
+// warp 0 TMA, warp 1 MMA (+TMEM), then EW screening warps: 4 (each thread one query, all 128
+// columns of a tile) or 8 (two threads per query, 64 columns each, two warps per scheduler)
+template <int EW>
+constexpr uint32_t kThreads = 64 + 32 * EW;
 constexpr uint32_t MAX_STAGES = 8;
 constexpr uint32_t TMEM_COLS = 2 * TN;  // two FP32 accumulators of 128 columns
 constexpr unsigned long long WAIT_CYCLES = 4000000000ull;  // about 2 s at 2 GHz
@@ -168,22 +171,24 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Inserts a key into a thread's sorted list of at most K2 keys (a full list drops its last key).
-// Lists are slot-major with a stride of 128 (the screening threads), so the threads of a warp
-// touch consecutive words.
+// Lists are slot-major with a stride of LS (the screening threads), so the threads of a warp touch
+// consecutive words.
+template <uint32_t LS>
 __device__ __forceinline__ void insert_key(uint64_t* list, uint32_t t, uint32_t K2, uint32_t& lcnt, uint64_t key) {
-  if (lcnt == K2 && key >= list[(K2 - 1) * TM + t]) return;
+  if (lcnt == K2 && key >= list[(K2 - 1) * LS + t]) return;
   uint32_t j = lcnt < K2 ? lcnt : K2 - 1;
   while (j > 0) {
-    const uint64_t prev = list[(j - 1) * TM + t];
+    const uint64_t prev = list[(j - 1) * LS + t];
     if (prev <= key) break;
-    list[j * TM + t] = prev;
+    list[j * LS + t] = prev;
     --j;
   }
-  list[j * TM + t] = key;
+  list[j * LS + t] = key;
   if (lcnt < K2) ++lcnt;
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
+template <int EW>
+__global__ void __launch_bounds__(kThreads<EW>, 1)
     tc_knn_kernel(const __grid_constant__ CUtensorMap mq_hi, const __grid_constant__ CUtensorMap mq_lo,
                   const __grid_constant__ CUtensorMap mx_hi, const __grid_constant__ CUtensorMap mx_lo,
                   const TcArgs a) {
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_addr(&bar_tfull[b]), 1);
-      mbar_init(smem_addr(&bar_tempty[b]), TM);
+      mbar_init(smem_addr(&bar_tempty[b]), 32 * EW);
     }
     mbar_init(smem_addr(&bar_drain), 1);
     abort_sh = 0;
@@ -302,16 +307,22 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
     }
   } else {
-    // ---------------------------------------------------------------- screening (warps 2-5)
-    const uint32_t quad = warp & 3u;       // TMEM lanes 32 * quad .. + 31
-    const uint32_t et = quad * 32 + lane;  // this thread's query within the tile
+    // ---------------------------------------------------------------- screening (warps 2 ..)
+    constexpr uint32_t CH = EW / 4;             // column parts of a tile (threads per query)
+    constexpr uint32_t CPT = TN / CH;           // columns per thread per tile
+    constexpr uint32_t LS = 32 * EW;            // list stride: all screening threads
+    const uint32_t ew = warp - 2;
+    const uint32_t quad = warp & 3u;            // TMEM lanes 32 * quad .. + 31
+    const uint32_t et = quad * 32 + lane;       // this thread's query within the tile
+    const uint32_t cp = ew / 4;                 // its column part: columns cp * CPT ..
+    const uint32_t lt = cp * TM + et;           // its list
     uint64_t* list = reinterpret_cast<uint64_t*>(smem + a.o_list);
-    // this thread's copy of a group's 64 values: float4 slot j4 stored at j4 ^ (et & 15), so that the
-    // eight threads of a quarter warp write different banks
-    float* scr = reinterpret_cast<float*>(smem + a.o_scr) + et * SCR;
-    const uint32_t sw = et & 15u;
+    // this thread's copy of a group's 16 values, float4 slot j4 stored at j4 ^ ((lane >> 1) & 3): the
+    // eight threads of a quarter warp then write eight different 16-byte bank groups
+    float* scr = reinterpret_cast<float*>(smem + a.o_scr) + (ew * 32 + lane) * GRP;
+    const uint32_t sw = (lane >> 1) & 3u;
     // base-row norms of the current and the next tile, one copy per warp (warp-local hand-over)
-    float* xw = reinterpret_cast<float*>(smem + a.o_xn) + (warp - 2) * 2 * TN;
+    float* xw = reinterpret_cast<float*>(smem + a.o_xn) + ew * 2 * TN;
     uint32_t tcount = 0;
     bool ok = true;
     for (uint32_t w = blockIdx.x; ok && w < items; w += gridDim.x) {
@@ -325,7 +336,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t lcnt = 0;
       // distance bound: the K2-th key's once the list is full; a thread past the queries accepts nothing
       float thr = qvalid ? (a.qbound ? a.qbound[q] : INFINITY) : -1.f;
-      // the mask test compares xn - 2 q.x against thr - qn, widened by a few ulps so that it never
+      // the group test compares xn - 2 q.x against thr - qn, widened by a few ulps so that it never
       // rejects what the exact test (d = xn - 2 q.x + qn <= thr) accepts
       auto bound = [&](float t) { return qvalid ? t - qn + (fabsf(t) + qn) * 4.8e-7f : -INFINITY; };
       float lim = bound(thr);
@@ -343,56 +354,63 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (!ok) break;
         tc_fence_after();
         const bool edge = row0 + TN > r1 || (self >= row0 && self < row0 + TN);
-        const uint32_t taddr = tmem_base + ((quad * 32u) << 16) + b * TN;
-        const float* xs = xw + (tcount & 1u) * TN;
+        const uint32_t taddr = tmem_base + ((quad * 32u) << 16) + b * TN + cp * CPT;
+        const float* xs = xw + (tcount & 1u) * TN + cp * CPT;
         uint32_t va[64], vb[64];
         tmem_ld64(taddr, va);
         tmem_wait();
-        tmem_ld64(taddr + 64, vb);  // the second half arrives while the first is screened
+        if (CPT == 128) tmem_ld64(taddr + 64, vb);  // the second half arrives while the first is screened
 #pragma unroll
-        for (uint32_t half = 0; half < 2; ++half) {
+        for (uint32_t half = 0; half < CPT / 64; ++half) {
           if (half == 1) tmem_wait();
           const uint32_t* v = half == 0 ? va : vb;
-          const float4* x4 = reinterpret_cast<const float4*>(xs + half * 64);
-          uint32_t m0 = 0, m1 = 0;  // values 0-31 and 32-63 under the bound
 #pragma unroll
-          for (uint32_t j4 = 0; j4 < 16; ++j4) {
-            const float4 xn = x4[j4];
-            const uint32_t bits = (fmaf(-2.f, __uint_as_float(v[4 * j4 + 0]), xn.x) <= lim ? 1u : 0u) |
-                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 1]), xn.y) <= lim ? 2u : 0u) |
-                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 2]), xn.z) <= lim ? 4u : 0u) |
-                                  (fmaf(-2.f, __uint_as_float(v[4 * j4 + 3]), xn.w) <= lim ? 8u : 0u);
-            if (j4 < 8) m0 |= bits << (4 * j4);
-            else m1 |= bits << (4 * (j4 - 8));
-          }
-          if (__any_sync(0xffffffffu, (m0 | m1) != 0u)) {
-            if ((m0 | m1) != 0u) {
+          for (uint32_t g = 0; g < 64 / GRP; ++g) {
+            const float4* x4 = reinterpret_cast<const float4*>(xs + half * 64 + g * GRP);
+            // any value of the group under the bound? (four independent chains)
+            bool h0 = false, h1 = false, h2 = false, h3 = false;
 #pragma unroll
-              for (uint32_t j4 = 0; j4 < 16; ++j4)
-                reinterpret_cast<float4*>(scr)[j4 ^ sw] =
-                    make_float4(__uint_as_float(v[4 * j4]), __uint_as_float(v[4 * j4 + 1]),
-                                __uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3]));
+            for (uint32_t j4 = 0; j4 < GRP / 4; ++j4) {
+              const float4 xn = x4[j4];
+              const uint32_t o = g * GRP + 4 * j4;
+              h0 |= fmaf(-2.f, __uint_as_float(v[o + 0]), xn.x) <= lim;
+              h1 |= fmaf(-2.f, __uint_as_float(v[o + 1]), xn.y) <= lim;
+              h2 |= fmaf(-2.f, __uint_as_float(v[o + 2]), xn.z) <= lim;
+              h3 |= fmaf(-2.f, __uint_as_float(v[o + 3]), xn.w) <= lim;
             }
-            // one marked value per lane per round, exact test, straight into the sorted list
-            while (__any_sync(0xffffffffu, (m0 | m1) != 0u)) {
-              if ((m0 | m1) != 0u) {
-                uint32_t j;
-                if (m0) {
-                  j = __ffs(m0) - 1;
-                  m0 &= m0 - 1;
-                } else {
-                  j = 32 + __ffs(m1) - 1;
-                  m1 &= m1 - 1;
+            const bool hit = h0 | h1 | h2 | h3;
+            if (__any_sync(0xffffffffu, hit)) {
+              // the group's values under the bound, as a mask; this thread's values to its scratch
+              uint32_t m = 0;
+              if (hit) {
+#pragma unroll
+                for (uint32_t j4 = 0; j4 < GRP / 4; ++j4) {
+                  const float4 xn = x4[j4];
+                  const uint32_t o = g * GRP + 4 * j4;
+                  m |= (fmaf(-2.f, __uint_as_float(v[o + 0]), xn.x) <= lim ? 1u : 0u) << (4 * j4);
+                  m |= (fmaf(-2.f, __uint_as_float(v[o + 1]), xn.y) <= lim ? 2u : 0u) << (4 * j4);
+                  m |= (fmaf(-2.f, __uint_as_float(v[o + 2]), xn.z) <= lim ? 4u : 0u) << (4 * j4);
+                  m |= (fmaf(-2.f, __uint_as_float(v[o + 3]), xn.w) <= lim ? 8u : 0u) << (4 * j4);
+                  reinterpret_cast<float4*>(scr)[j4 ^ sw] =
+                      make_float4(__uint_as_float(v[o]), __uint_as_float(v[o + 1]), __uint_as_float(v[o + 2]),
+                                  __uint_as_float(v[o + 3]));
                 }
-                const float val = scr[(((j >> 2) ^ sw) << 2) | (j & 3u)];
-                const uint32_t c = half * 64 + j;
-                const float d = fmaxf(fmaf(-2.f, val, xs[c]) + qn, 0.f);
-                const uint64_t row = row0 + c;
-                if (d <= thr && (!edge || (row < r1 && row != self))) {
-                  insert_key(list, et, a.K2, lcnt, ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)row);
-                  if (lcnt == a.K2) {
-                    thr = __uint_as_float((uint32_t)(list[(a.K2 - 1) * TM + et] >> 32));
-                    lim = bound(thr);
+              }
+              // one marked value per lane per round: the exact test, straight into the sorted list
+              while (__any_sync(0xffffffffu, m != 0u)) {
+                if (m != 0u) {
+                  const uint32_t j = __ffs(m) - 1;
+                  m &= m - 1;
+                  const float val = scr[(((j >> 2) ^ sw) << 2) | (j & 3u)];
+                  const uint32_t c = half * 64 + g * GRP + j;
+                  const float d = fmaxf(fmaf(-2.f, val, xs[c]) + qn, 0.f);
+                  const uint64_t row = row0 + cp * CPT + c;
+                  if (d <= thr && (!edge || (row < r1 && row != self))) {
+                    insert_key<LS>(list, lt, a.K2, lcnt, ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)row);
+                    if (lcnt == a.K2) {
+                      thr = __uint_as_float((uint32_t)(list[(a.K2 - 1) * LS + lt] >> 32));
+                      lim = bound(thr);
+                    }
                   }
                 }
               }
@@ -405,9 +423,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         __syncwarp();
       }
       if (!ok) break;
-      if (qvalid) {
-        uint64_t* dst = a.part + ((uint64_t)q * a.nchunks + chunk) * a.K2;
-        for (uint32_t i = 0; i < a.K2; ++i) dst[i] = i < lcnt ? list[i * TM + et] : ~0ull;
+      if (qvalid) {  // list part cp of this (query, chunk): the merge sees CH lists per chunk
+        uint64_t* dst = a.part + ((uint64_t)q * a.nchunks * CH + chunk * CH + cp) * a.K2;
+        for (uint32_t i = 0; i < a.K2; ++i) dst[i] = i < lcnt ? list[i * LS + lt] : ~0ull;
       }
     }
   }
@@ -478,14 +496,34 @@ __global__ void sample_rows_kernel(const uint4* __restrict__ hi, const uint4* __
   }
 }
 
-// Per query the distance of the rank-th key of its list (nq lists of `stride` keys), widened by
-// `rel` (the split form's two passes may round differently); +inf when the list is shorter.
-__global__ void bound_kernel(const uint64_t* __restrict__ lists, uint64_t nq, uint32_t stride, uint32_t rank,
-                             float rel, float* __restrict__ out) {
+// Per query the distance of the rank-th smallest key over its L sorted lists of `stride` keys (L =
+// 1 or 2, ~0 padded), widened by `rel` (the split form's passes may round differently); +inf when
+// the lists hold fewer keys; never above the query's previous bound `prev` (when given).
+__global__ void bound_kernel(const uint64_t* __restrict__ lists, uint64_t nq, uint32_t L, uint32_t stride,
+                             uint32_t rank, float rel, const float* __restrict__ prev, float* __restrict__ out) {
   for (uint64_t qi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = lists[qi * stride + rank - 1];
+    const uint64_t* a = lists + qi * L * stride;
+    uint64_t key = ~0ull;
+    if (L == 1) {
+      key = a[rank - 1];
+    } else {  // merge walk over the two lists up to the rank-th key
+      const uint64_t* b = a + stride;
+      uint32_t i = 0, j = 0;
+      for (uint32_t r = 0; r < rank; ++r) {
+        const uint64_t x = i < stride ? a[i] : ~0ull, y = j < stride ? b[j] : ~0ull;
+        if (x <= y) {
+          key = x;
+          ++i;
+        } else {
+          key = y;
+          ++j;
+        }
+      }
+    }
     const float d = __uint_as_float((uint32_t)(key >> 32));
-    out[qi] = key == ~0ull ? INFINITY : d + d * rel;
+    float bnd = key == ~0ull ? INFINITY : d + d * rel;
+    if (prev) bnd = fminf(bnd, prev[qi]);
+    out[qi] = bnd;
   }
 }
 
@@ -552,15 +590,11 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   __nv_bfloat16 *xh = nullptr, *xl = nullptr, *qh = nullptr, *ql = nullptr;
   float *xn = nullptr, *qn = nullptr;
   int* flags = nullptr;
-  uint64_t *part = nullptr, *part0 = nullptr;
-  __nv_bfloat16 *sh = nullptr, *sl = nullptr;
+  uint64_t* part = nullptr;
   float *sn = nullptr, *qbound = nullptr;
   auto release = [&] {
-    cudaFreeAsync(sh, s);
-    cudaFreeAsync(sl, s);
     cudaFreeAsync(sn, s);
     cudaFreeAsync(qbound, s);
-    cudaFreeAsync(part0, s);
     cudaFreeAsync(xh, s);
     cudaFreeAsync(xl, s);
     cudaFreeAsync(qh, s);
@@ -608,15 +642,18 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
 
   // shared memory: pipeline stages, then the per-thread lists, scratch and norm copies
   const uint32_t stage_bytes = 2 * PART;
+  // screening warps: eight (two threads per query) while their lists fit, else four
+  auto warps_for = [](uint32_t K2l) { return K2l <= 48 ? 8u : 4u; };
   auto layout = [&](uint32_t K2l, uint32_t& stages, uint32_t& o_list, uint32_t& o_scr, uint32_t& o_xn,
                     size_t& smem) -> bool {
-    const uint32_t epi = TM * K2l * 8 + TM * SCR * 4 + 4 * 2 * TN * 4;
-    const int64_t room = (int64_t)smem_max - 1024 - 2048 - epi;  // alignment pad, static barriers
+    const uint32_t ew = warps_for(K2l);
+    const uint32_t lists = 32 * ew * K2l * 8, scratch = 32 * ew * GRP * 4, norms = ew * 2 * TN * 4;
+    const int64_t room = (int64_t)smem_max - 1024 - 2048 - lists - scratch - norms;  // alignment pad, barriers
     stages = (uint32_t)std::min<int64_t>(MAX_STAGES, std::max<int64_t>(0, room / stage_bytes));
     o_list = stages * stage_bytes;
-    o_scr = o_list + TM * K2l * 8;
-    o_xn = o_scr + TM * SCR * 4;
-    smem = 1024 + (size_t)o_xn + 4 * 2 * TN * 4;
+    o_scr = o_list + lists;
+    o_xn = o_scr + scratch;
+    smem = 1024 + (size_t)o_xn + norms;
     return stages >= 2;
   };
   auto launch = [&](const CUtensorMap& mq_h, const CUtensorMap& mq_l, const CUtensorMap& mx_h,
@@ -646,9 +683,14 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
     a.o_list = o_list;
     a.o_scr = o_scr;
     a.o_xn = o_xn;
-    EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned grid = (unsigned)std::min<uint64_t>(qtiles * nch, (uint64_t)sms);
-    tc_knn_kernel<<<grid, THREADS, smem, s>>>(mq_h, mq_l, mx_h, mx_l, a);
+    if (warps_for(K2l) == 8) {
+      EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      tc_knn_kernel<8><<<grid, kThreads<8>, smem, s>>>(mq_h, mq_l, mx_h, mx_l, a);
+    } else {
+      EFG_CUDA(cudaFuncSetAttribute(tc_knn_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      tc_knn_kernel<4><<<grid, kThreads<4>, smem, s>>>(mq_h, mq_l, mx_h, mx_l, a);
+    }
     EFG_CUDA(cudaGetLastError());
     if (grid_out) *grid_out = grid;
     g_knn_stats.stages = stages;
@@ -666,36 +708,63 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_TRY(make_map(&mxh, xh, n, W));
   EFG_TRY(make_map(&mxl, xl, n, W));
 
-  // 1. bound pass over a strided sample of S base rows: the rank-th distance of the sample, rank =
-  // K2 (+ 1 with exclude_self: the sample may hold the query itself)
+  // 1. bounds from strided samples of the base: the rank-th distance of a sample bounds the whole
+  // base's (rank = K2, + 1 with exclude_self: a sample may hold the query itself).  A first pass over
+  // S0 rows, then one over S1 rows (S0 of them among them) that starts from the first bound.
   EFG_CUDA(cudaEventRecord(ev[1], s));
-  uint32_t S = (uint32_t)std::min<uint64_t>(65536, n / 16) / TN * TN;
   const uint32_t rank = K2 + (exclude_self ? 1u : 0u);
-  if (S >= 4096 && S >= rank) {
-    EFG_CUDA(cudaMallocAsync((void**)&sh, (uint64_t)S * W * 2, s));
-    EFG_CUDA(cudaMallocAsync((void**)&sl, (uint64_t)S * W * 2, s));
-    EFG_CUDA(cudaMallocAsync((void**)&sn, (uint64_t)S * 4, s));
-    EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
-    EFG_CUDA(cudaMallocAsync((void**)&part0, nq * rank * 8, s));
-    sample_rows_kernel<<<(unsigned)std::min<uint64_t>((S + 7) / 8, (uint64_t)sms * 8), 256, 0, s>>>(
-        reinterpret_cast<const uint4*>(xh), reinterpret_cast<const uint4*>(xl), xn, n, W, S,
-        reinterpret_cast<uint4*>(sh), reinterpret_cast<uint4*>(sl), sn);
+  const uint32_t CHb = warps_for(rank) / 4;
+  const uint32_t S0 = 4096;
+  uint32_t S1 = (uint32_t)std::min<uint64_t>(65536, n / 16) / S0 * S0;
+  uint32_t S = 0;  // rows of the last bound pass
+  auto bound_pass = [&](uint32_t rows, const float* prev, float* out) -> int {
+    __nv_bfloat16 *bh = nullptr, *bl = nullptr;
+    float* bn = nullptr;
+    uint64_t* lists = nullptr;
+    struct Free {
+      cudaStream_t s;
+      void* p[4];
+      ~Free() {
+        for (void* x : p) cudaFreeAsync(x, s);
+      }
+    } fr{s, {nullptr, nullptr, nullptr, nullptr}};
+    EFG_CUDA(cudaMallocAsync((void**)&bh, (uint64_t)rows * W * 2, s));
+    fr.p[0] = bh;
+    EFG_CUDA(cudaMallocAsync((void**)&bl, (uint64_t)rows * W * 2, s));
+    fr.p[1] = bl;
+    EFG_CUDA(cudaMallocAsync((void**)&bn, (uint64_t)rows * 4, s));
+    fr.p[2] = bn;
+    EFG_CUDA(cudaMallocAsync((void**)&lists, nq * CHb * rank * 8, s));
+    fr.p[3] = lists;
+    sample_rows_kernel<<<(unsigned)std::min<uint64_t>((rows + 7) / 8, (uint64_t)sms * 8), 256, 0, s>>>(
+        reinterpret_cast<const uint4*>(xh), reinterpret_cast<const uint4*>(xl), xn, n, W, rows,
+        reinterpret_cast<uint4*>(bh), reinterpret_cast<uint4*>(bl), bn);
     EFG_CUDA(cudaGetLastError());
-    CUtensorMap msh, msl;
-    EFG_TRY(make_map(&msh, sh, S, W));
-    EFG_TRY(make_map(&msl, sl, S, W));
-    EFG_TRY(launch(mqh, mql, msh, msl, sn, S, S, 1, rank, nullptr, part0, 0, nullptr));
+    CUtensorMap mbh, mbl;
+    EFG_TRY(make_map(&mbh, bh, rows, W));
+    EFG_TRY(make_map(&mbl, bl, rows, W));
+    EFG_TRY(launch(mqh, mql, mbh, mbl, bn, rows, rows, 1, rank, prev, lists, 0, nullptr));
     bound_kernel<<<(unsigned)std::min<uint64_t>((nq + 255) / 256, 4096), 256, 0, s>>>(
-        part0, nq, rank, rank, terms == 1 ? 0.f : 1e-5f, qbound);
+        lists, nq, CHb, rank, rank, terms == 1 ? 0.f : 1e-5f, prev, out);
     EFG_CUDA(cudaGetLastError());
-  } else {
-    S = 0;
+    S = rows;
+    return EFG_OK;
+  };
+  if (n / 16 >= S0 && S0 >= rank) {
+    EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
+    EFG_TRY(bound_pass(S0, nullptr, qbound));
+    if (S1 >= 4 * S0) {
+      EFG_CUDA(cudaMallocAsync((void**)&sn, nq * 4, s));  // the second bound, then swapped in
+      EFG_TRY(bound_pass(S1, qbound, sn));
+      std::swap(sn, qbound);
+    }
   }
 
   // 2. the whole base in (query tile, base chunk) items, about 8 per SM, balanced over the SMs
   uint64_t best_nc = 1;
   double best_cost = 1e300;
-  const uint64_t max_nc = std::max<uint64_t>(1, std::min<uint64_t>(4096 / K2, (n + TN - 1) / TN));
+  const uint32_t CH = warps_for(K2) / 4;  // lists per (query, chunk)
+  const uint64_t max_nc = std::max<uint64_t>(1, std::min<uint64_t>(4096 / (K2 * CH), (n + TN - 1) / TN));
   const uint64_t target = std::max<uint64_t>(1, ((uint64_t)sms * 8 + qtiles - 1) / qtiles);
   for (uint64_t nc = std::max<uint64_t>(1, target / 2); nc <= std::min(max_nc, target * 2); ++nc) {
     const uint64_t chunk = ((n + nc - 1) / nc + TN - 1) / TN * TN;
@@ -710,12 +779,12 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   }
   const uint64_t chunk = ((n + best_nc - 1) / best_nc + TN - 1) / TN * TN;
   const uint32_t nchunks = (uint32_t)((n + chunk - 1) / chunk);
-  EFG_CUDA(cudaMallocAsync((void**)&part, nq * nchunks * K2 * 8, s));
+  EFG_CUDA(cudaMallocAsync((void**)&part, nq * nchunks * CH * K2 * 8, s));
   EFG_CUDA(cudaEventRecord(ev[2], s));
   unsigned grid = 0;
   EFG_TRY(launch(mqh, mql, mxh, mxl, xn, n, chunk, nchunks, K2, S ? qbound : nullptr, part, exclude_self, &grid));
   EFG_CUDA(cudaEventRecord(ev[3], s));
-  EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks, part, ids, dists, s));
+  EFG_TRY(bf_merge_launch(base, dim, ld, q, nq, qld, k, K2, nchunks * CH, part, ids, dists, s));
   EFG_CUDA(cudaEventRecord(ev[4], s));
   EFG_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, s));
   EFG_CUDA(cudaStreamSynchronize(s));

@@ -253,26 +253,54 @@ __global__ void __launch_bounds__(BF_THREADS) bf_chunk_kernel(const float* __res
   }
 }
 
-// Merges the per-chunk lists of one query (one warp per query) and re-ranks in FP64.
+// Merges the per-chunk lists of one query (one warp per query) and re-ranks in FP64.  Each list is
+// sorted ascending (~0 padded), so the K2 smallest keys overall are taken head by head: lane l
+// follows lists l, l + 32, ..., and each round the warp minimum of the lanes' best heads is taken
+// and its list advanced (keys are distinct: ids differ across chunks).
 __global__ void bf_merge_kernel(const float* __restrict__ base, uint32_t dim, uint32_t ld,
                                 const float* __restrict__ q, uint64_t nq, uint32_t qld, uint32_t k, uint32_t K2,
-                                uint32_t nchunks, const uint64_t* __restrict__ part, int32_t* __restrict__ ids,
+                                uint32_t nlists, const uint64_t* __restrict__ part, int32_t* __restrict__ ids,
                                 float* __restrict__ dists) {
   extern __shared__ __align__(16) unsigned char smem[];
   uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t wpb = blockDim.x >> 5;
   uint64_t qi = (uint64_t)blockIdx.x * wpb + warp;
-  uint32_t tot = nchunks * K2;
-  uint32_t p2 = 1;
-  while (p2 < tot) p2 <<= 1;
-  uint64_t* buf = reinterpret_cast<uint64_t*>(smem) + (size_t)warp * p2;
+  uint64_t* buf = reinterpret_cast<uint64_t*>(smem) + (size_t)warp * K2;  // the K2 selected keys
+  double* d64 = reinterpret_cast<double*>(smem + (size_t)wpb * K2 * 8) + (size_t)warp * K2;
+  uint32_t* pos = reinterpret_cast<uint32_t*>(smem + (size_t)wpb * K2 * 16) + (size_t)warp * nlists;
   if (qi >= nq) return;
-  const uint64_t* src = part + qi * tot;
-  for (uint32_t i = lane; i < p2; i += 32) buf[i] = i < tot ? src[i] : ~0ULL;
+  const uint64_t* src = part + qi * (uint64_t)nlists * K2;
+  for (uint32_t l = lane; l < nlists; l += 32) pos[l] = 0;
   __syncwarp();
-  warp_bitonic_sort(buf, p2);
-  // FP64 re-rank of the first K2 (ids are distinct across chunks)
-  double* d64 = reinterpret_cast<double*>(smem + (size_t)wpb * p2 * 8) + (size_t)warp * K2;
+  uint64_t hk = ~0ULL;  // this lane's smallest head and its list
+  uint32_t hl = 0;
+  auto lane_best = [&]() {
+    hk = ~0ULL;
+    for (uint32_t l = lane; l < nlists; l += 32) {
+      const uint32_t p = pos[l];
+      const uint64_t h = p < K2 ? src[(uint64_t)l * K2 + p] : ~0ULL;
+      if (h < hk) {
+        hk = h;
+        hl = l;
+      }
+    }
+  };
+  lane_best();
+  for (uint32_t r = 0; r < K2; ++r) {
+    uint64_t m = hk;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const uint64_t other = __shfl_xor_sync(0xffffffffu, m, o);
+      m = other < m ? other : m;
+    }
+    if (lane == 0) buf[r] = m;
+    if (m != ~0ULL && hk == m) {  // the lane holding the minimum advances that list
+      pos[hl] += 1;
+      lane_best();
+    }
+    __syncwarp();
+  }
+  // FP64 re-rank of the K2 selected keys
   const float* qr = q + qi * qld;
   for (uint32_t i = 0; i < K2; ++i) {
     uint64_t key = buf[i];
@@ -313,17 +341,15 @@ __global__ void bf_merge_kernel(const float* __restrict__ base, uint32_t dim, ui
   }
 }
 
-// Launches the merge of the per-(query, chunk) lists `part` (nq x nchunks x K2 keys): per query the
-// K2 smallest keys, re-ranked in FP64, of which the k first go to ids (and dists).
+// Launches the merge of the per-(query, chunk) lists `part` (nq x nlists x K2 keys, each list sorted):
+// per query the K2 smallest keys, re-ranked in FP64, of which the k first go to ids (and dists).
 int bf_merge_launch(const float* base, uint32_t dim, uint32_t ld, const float* q, uint64_t nq, uint32_t qld,
-                    uint32_t k, uint32_t K2, uint32_t nchunks, const uint64_t* part, int32_t* ids, float* dists,
+                    uint32_t k, uint32_t K2, uint32_t nlists, const uint64_t* part, int32_t* ids, float* dists,
                     cudaStream_t s) {
-  uint32_t tot = nchunks * K2, p2 = 1;
-  while (p2 < tot) p2 <<= 1;
-  uint32_t wpb = p2 <= 2048 ? 4 : 1;
-  size_t msmem = (size_t)wpb * p2 * 8 + (size_t)wpb * K2 * 8;
+  const uint32_t wpb = 4;
+  size_t msmem = (size_t)wpb * K2 * 16 + (size_t)wpb * nlists * 4;
   if (msmem > 48 * 1024) EFG_CUDA(cudaFuncSetAttribute(bf_merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem));
-  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2, nchunks,
+  bf_merge_kernel<<<(unsigned)((nq + wpb - 1) / wpb), wpb * 32, msmem, s>>>(base, dim, ld, q, nq, qld, k, K2, nlists,
                                                                             part, ids, dists);
   EFG_CUDA(cudaGetLastError());
   return EFG_OK;

@@ -496,29 +496,28 @@ __global__ void sample_rows_kernel(const uint4* __restrict__ hi, const uint4* __
   }
 }
 
-// Per query the distance of the rank-th smallest key over its L sorted lists of `stride` keys (L =
-// 1 or 2, ~0 padded), widened by `rel` (the split form's passes may round differently); +inf when
-// the lists hold fewer keys; never above the query's previous bound `prev` (when given).
+// Per query the distance of the rank-th smallest key over its L sorted lists of `stride` keys (L <=
+// 16, ~0 padded), widened by `rel` (the split form's passes may round differently); +inf when the
+// lists hold fewer keys; never above the query's previous bound `prev` (when given).
 __global__ void bound_kernel(const uint64_t* __restrict__ lists, uint64_t nq, uint32_t L, uint32_t stride,
                              uint32_t rank, float rel, const float* __restrict__ prev, float* __restrict__ out) {
   for (uint64_t qi = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t* a = lists + qi * L * stride;
+    uint32_t pos[16];
+    for (uint32_t l = 0; l < L; ++l) pos[l] = 0;
     uint64_t key = ~0ull;
-    if (L == 1) {
-      key = a[rank - 1];
-    } else {  // merge walk over the two lists up to the rank-th key
-      const uint64_t* b = a + stride;
-      uint32_t i = 0, j = 0;
-      for (uint32_t r = 0; r < rank; ++r) {
-        const uint64_t x = i < stride ? a[i] : ~0ull, y = j < stride ? b[j] : ~0ull;
-        if (x <= y) {
-          key = x;
-          ++i;
-        } else {
-          key = y;
-          ++j;
+    for (uint32_t r = 0; r < rank; ++r) {  // merge walk up to the rank-th key
+      uint32_t best = 0;
+      key = ~0ull;
+      for (uint32_t l = 0; l < L; ++l) {
+        const uint64_t h = pos[l] < stride ? a[l * stride + pos[l]] : ~0ull;
+        if (h < key) {
+          key = h;
+          best = l;
         }
       }
+      if (key == ~0ull) break;
+      pos[best] += 1;
     }
     const float d = __uint_as_float((uint32_t)(key >> 32));
     float bnd = key == ~0ull ? INFINITY : d + d * rel;
@@ -709,13 +708,12 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_TRY(make_map(&mxl, xl, n, W));
 
   // 1. bounds from strided samples of the base: the rank-th distance of a sample bounds the whole
-  // base's (rank = K2, + 1 with exclude_self: a sample may hold the query itself).  A first pass over
-  // S0 rows, then one over S1 rows (S0 of them among them) that starts from the first bound.
+  // base's (rank = K2, + 1 with exclude_self: a sample may hold the query itself).  Samples of S0 <
+  // S1 < S2 rows, each holding the previous one (strides that divide), each pass starting from the
+  // previous bound so that it only admits about rank x (its rows / the previous rows) candidates.
   EFG_CUDA(cudaEventRecord(ev[1], s));
   const uint32_t rank = K2 + (exclude_self ? 1u : 0u);
   const uint32_t CHb = warps_for(rank) / 4;
-  const uint32_t S0 = 4096;
-  uint32_t S1 = (uint32_t)std::min<uint64_t>(65536, n / 16) / S0 * S0;
   uint32_t S = 0;  // rows of the last bound pass
   auto bound_pass = [&](uint32_t rows, const float* prev, float* out) -> int {
     __nv_bfloat16 *bh = nullptr, *bl = nullptr;
@@ -728,13 +726,18 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
         for (void* x : p) cudaFreeAsync(x, s);
       }
     } fr{s, {nullptr, nullptr, nullptr, nullptr}};
+    // chunks: enough items for the SMs, at most 16 lists per query, at least 1024 rows each
+    uint32_t nch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((sms + qtiles - 1) / qtiles, 16 / CHb));
+    nch = std::min<uint32_t>(nch, std::max<uint32_t>(1, rows / 1024));
+    const uint32_t crow = (rows / nch + TN - 1) / TN * TN;
+    nch = (rows + crow - 1) / crow;
     EFG_CUDA(cudaMallocAsync((void**)&bh, (uint64_t)rows * W * 2, s));
     fr.p[0] = bh;
     EFG_CUDA(cudaMallocAsync((void**)&bl, (uint64_t)rows * W * 2, s));
     fr.p[1] = bl;
     EFG_CUDA(cudaMallocAsync((void**)&bn, (uint64_t)rows * 4, s));
     fr.p[2] = bn;
-    EFG_CUDA(cudaMallocAsync((void**)&lists, nq * CHb * rank * 8, s));
+    EFG_CUDA(cudaMallocAsync((void**)&lists, nq * nch * CHb * rank * 8, s));
     fr.p[3] = lists;
     sample_rows_kernel<<<(unsigned)std::min<uint64_t>((rows + 7) / 8, (uint64_t)sms * 8), 256, 0, s>>>(
         reinterpret_cast<const uint4*>(xh), reinterpret_cast<const uint4*>(xl), xn, n, W, rows,
@@ -743,19 +746,26 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
     CUtensorMap mbh, mbl;
     EFG_TRY(make_map(&mbh, bh, rows, W));
     EFG_TRY(make_map(&mbl, bl, rows, W));
-    EFG_TRY(launch(mqh, mql, mbh, mbl, bn, rows, rows, 1, rank, prev, lists, 0, nullptr));
-    bound_kernel<<<(unsigned)std::min<uint64_t>((nq + 255) / 256, 4096), 256, 0, s>>>(
-        lists, nq, CHb, rank, rank, terms == 1 ? 0.f : 1e-5f, prev, out);
+    EFG_TRY(launch(mqh, mql, mbh, mbl, bn, rows, crow, nch, rank, prev, lists, 0, nullptr));
+    bound_kernel<<<(unsigned)std::min<uint64_t>((nq + 127) / 128, 4096), 128, 0, s>>>(
+        lists, nq, nch * CHb, rank, rank, terms == 1 ? 0.f : 1e-5f, prev, out);
     EFG_CUDA(cudaGetLastError());
     S = rows;
     return EFG_OK;
   };
+  // sample sizes: multiples of each other (so each sample holds the previous one) and of 128
+  const uint32_t S2 = (uint32_t)std::min<uint64_t>(65536, n / 16) / 16384 * 16384;
+  const uint32_t S1 = 16384, S0 = 2048;
   if (n / 16 >= S0 && S0 >= rank) {
     EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
+    EFG_CUDA(cudaMallocAsync((void**)&sn, nq * 4, s));
     EFG_TRY(bound_pass(S0, nullptr, qbound));
-    if (S1 >= 4 * S0) {
-      EFG_CUDA(cudaMallocAsync((void**)&sn, nq * 4, s));  // the second bound, then swapped in
+    if (n / 16 >= S1) {
       EFG_TRY(bound_pass(S1, qbound, sn));
+      std::swap(sn, qbound);
+    }
+    if (S2 >= 2 * S1) {
+      EFG_TRY(bound_pass(S2, qbound, sn));
       std::swap(sn, qbound);
     }
   }

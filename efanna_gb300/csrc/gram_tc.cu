@@ -708,9 +708,9 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
   EFG_TRY(make_map(&mxl, xl, n, W));
 
   // 1. bounds from strided samples of the base: the rank-th distance of a sample bounds the whole
-  // base's (rank = K2, + 1 with exclude_self: a sample may hold the query itself).  Samples of S0 <
-  // S1 < S2 rows, each holding the previous one (strides that divide), each pass starting from the
-  // previous bound so that it only admits about rank x (its rows / the previous rows) candidates.
+  // base's (rank = K2, + 1 with exclude_self: a sample may hold the query itself).  Nested samples
+  // growing 8x, each holding the previous one (strides that divide), each pass starting from the
+  // previous bound so that it only admits about 8 x rank candidates.
   EFG_CUDA(cudaEventRecord(ev[1], s));
   const uint32_t rank = K2 + (exclude_self ? 1u : 0u);
   const uint32_t CHb = warps_for(rank) / 4;
@@ -753,19 +753,16 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
     S = rows;
     return EFG_OK;
   };
-  // sample sizes: multiples of each other (so each sample holds the previous one) and of 128
-  const uint32_t S2 = (uint32_t)std::min<uint64_t>(65536, n / 16) / 16384 * 16384;
-  const uint32_t S1 = 16384, S0 = 2048;
-  if (n / 16 >= S0 && S0 >= rank) {
+  // sample sizes: S0 = 64 x rank (at least 2048) and 8x steps up to n / 16, each a multiple of the
+  // previous one (so each sample holds the previous one) and of the tile height
+  uint32_t S0 = 2048;
+  while (S0 < 64 * rank) S0 *= 2;
+  if (n / 16 >= S0) {
     EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
     EFG_CUDA(cudaMallocAsync((void**)&sn, nq * 4, s));
     EFG_TRY(bound_pass(S0, nullptr, qbound));
-    if (n / 16 >= S1) {
-      EFG_TRY(bound_pass(S1, qbound, sn));
-      std::swap(sn, qbound);
-    }
-    if (S2 >= 2 * S1) {
-      EFG_TRY(bound_pass(S2, qbound, sn));
+    for (uint64_t Si = (uint64_t)S0 * 8; Si <= std::min<uint64_t>(n / 16, 1u << 20); Si *= 8) {
+      EFG_TRY(bound_pass((uint32_t)Si, qbound, sn));
       std::swap(sn, qbound);
     }
   }

@@ -761,8 +761,15 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
     EFG_CUDA(cudaMallocAsync((void**)&qbound, nq * 4, s));
     EFG_CUDA(cudaMallocAsync((void**)&sn, nq * 4, s));
     EFG_TRY(bound_pass(S0, nullptr, qbound));
-    for (uint64_t Si = (uint64_t)S0 * 8; Si <= std::min<uint64_t>(n / 16, 1u << 20); Si *= 8) {
+    uint64_t last = S0;
+    const uint64_t cap = std::min<uint64_t>(n / 16, 1u << 20);
+    for (uint64_t Si = last * 8; Si <= cap; Si *= 8) {
       EFG_TRY(bound_pass((uint32_t)Si, qbound, sn));
+      std::swap(sn, qbound);
+      last = Si;
+    }
+    if (cap / last >= 2) {  // the largest multiple of the last sample within n / 16
+      EFG_TRY(bound_pass((uint32_t)(cap / last * last), qbound, sn));
       std::swap(sn, qbound);
     }
   }

@@ -10,8 +10,10 @@
 // the library holds these 16 MiB until the process exits.
 //
 // The array's name in host code is only a host-side stand-in, not a device address; the device
-// address is looked up with cudaGetSymbolAddress once per device, on the first call made with
-// that device current, and cached.  That first call should come before any stream capture.
+// address is looked up with cudaGetSymbolAddress on the first call made with a device (and
+// context) current, and cached per device together with that context; a call from another context
+// on the same device (after cudaDeviceReset, or a context made through the driver API) looks it up
+// again.  That first call per device and context should come before any stream capture.
 // All calls share the one array: calls that overlap on the GPU (concurrent streams, or threads
 // sharing a device) race on it and must be serialised by the caller.  Nothing in it needs to start
 // at zero -- every entry the second kernel reads is written by the first kernel of the same call.
@@ -32,21 +34,46 @@ static __device__ __align__(256) uint64_t g_bf_scratch[kScratchEntries];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// Per device ordinal: the context the address was looked up in, and the address.  A call made in
+// another context on the same ordinal (after cudaDeviceReset, or with a context the caller created
+// through the driver API) looks the address up again in that context.
+void* g_ctx[kMaxDevices] = {};
 uint64_t* g_dev_ptr[kMaxDevices] = {};
 
-// Device address of g_bf_scratch on the current device (looked up once per device).
+// cuCtxGetCurrent from the driver, found once through the runtime (no link against libcuda).
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static std::once_flag once;
+  static CtxGetCurrentFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
+
+// Device address of g_bf_scratch in the current device's current context.
 int scratch_address(uint64_t** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return efg::fail(EFG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return efg::fail(EFG_ERR_ARG, "device ordinal beyond the scratch table");
+  e = cudaFree(nullptr);  // makes the runtime's context current on this thread if none is
+  if (e != cudaSuccess) return efg::fail(EFG_ERR_CUDA, std::string("cudaFree(0): ") + cudaGetErrorString(e));
+  void* ctx = nullptr;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get || get(&ctx) != 0 || !ctx) return efg::fail(EFG_ERR_CUDA, "no current CUDA context");
   std::lock_guard<std::mutex> g(g_mu);
-  if (!g_dev_ptr[dev]) {
+  if (!g_dev_ptr[dev] || g_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_bf_scratch);
     if (e != cudaSuccess || !p)
       return efg::fail(EFG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
     g_dev_ptr[dev] = static_cast<uint64_t*>(p);
+    g_ctx[dev] = ctx;
   }
   *out = g_dev_ptr[dev];
   return EFG_OK;

@@ -366,8 +366,11 @@ int efg_brute_force_knn_split(const float* d_base, uint64_t n, uint32_t dim, uin
  * the library (EFG_BF_NOALLOC_SCRATCH_ENTRIES 8-byte entries = 16 MiB, held on every GPU that loads
  * the library until exit); calls needing more than nq * (k + 16) <= that many entries return
  * EFG_ERR_ARG.  The first call on a device looks up the scratch address (cudaGetSymbolAddress),
- * so make it before any stream capture.  All calls share the scratch: calls that overlap on the
- * GPU race and must be serialised by the caller. */
+ * so make it before any stream capture; the address is kept per device and CUDA context, and a
+ * call from a new context on that device (after cudaDeviceReset, or a driver-API context) looks it
+ * up again -- also before any capture in that context.  All calls share the scratch: calls that
+ * overlap on the GPU race and must be serialised by the caller.  Screening here is the FP32 kernel
+ * of efg_brute_force_knn_fp32 (same results as efg_brute_force_knn). */
 #define EFG_BF_NOALLOC_SCRATCH_ENTRIES (1ull << 21)
 int efg_brute_force_knn_noalloc(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride,
                                 const float* d_q, uint64_t nq, uint64_t q_stride, uint32_t k, int exclude_self,

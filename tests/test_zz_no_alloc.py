@@ -57,3 +57,32 @@ def test_noalloc_float_data_and_size_limit(efg):
                                          64, 256, 0, 0, C.c_void_p(ids.data_ptr()), None, None)
     assert rc == efg.EFG_ERR_ARG
     assert b"scratch" in lib.efg_last_error()
+
+
+def test_noalloc_strides_exclude_self_and_stream(efg):
+    """Padded rows (dim 33 in rows of 36 floats, queries in rows of 40), exclude_self with a
+    non-zero first row, and a call on a non-default stream: the same ids and distances as the
+    allocating entry point, whose smaller chunk count the fixed scratch may force."""
+    torch = pytest.importorskip("torch")
+    lib = efg.lib()
+    x = datasets.mixture_u8(6000, 33, seed=12)
+    xp = np.zeros((6000, 36), np.float32)
+    xp[:, :33] = x
+    first = 2500
+    qp = np.zeros((700, 40), np.float32)
+    qp[:, :33] = x[first:first + 700]
+    X, Q = torch.from_numpy(xp).cuda(), torch.from_numpy(qp).cuda()
+    s = torch.cuda.Stream()
+    out = {}
+    for name, stream in (("efg_brute_force_knn", None), ("efg_brute_force_knn_noalloc", s.cuda_stream)):
+        ids = torch.full((700, 16), -7, dtype=torch.int32, device="cuda")
+        dist = torch.full((700, 16), -1.0, dtype=torch.float32, device="cuda")
+        rc = getattr(lib, name)(C.c_void_p(X.data_ptr()), 6000, 33, 36, C.c_void_p(Q.data_ptr()), 700, 40, 16, 1, first,
+                                C.c_void_p(ids.data_ptr()), C.c_void_p(dist.data_ptr()),
+                                C.c_void_p(stream) if stream else None)
+        torch.cuda.synchronize()
+        assert rc == 0, lib.efg_last_error()
+        out[name] = (ids.cpu().numpy(), dist.cpu().numpy())
+    want, got = out["efg_brute_force_knn"], out["efg_brute_force_knn_noalloc"]
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    assert not np.any(got[0] == (first + np.arange(700))[:, None])

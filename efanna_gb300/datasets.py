@@ -10,8 +10,15 @@ same shapes and value ranges:
 * ``mixture_unit``: a Dirichlet-weighted mixture of non-negative components with values in
   [0, 1] and L1-normalised blocks (GIST-like, for the high-dimensional precision workload).
 
+* ``mixture_unit_device``: the same GIST-like family drawn on the GPU with torch's seeded
+  generator (the 1M x 960 workload: numpy's gamma draws would take tens of seconds on the host).
+* ``mixture_aniso_device``: a Gaussian mixture with anisotropic covariances -- per component a
+  random rotation times a decaying spectrum -- drawn on the GPU (the 10M x 96 workload of the
+  learned form).
+
 Base points use ``seed`` and queries ``seed + 1``; the mixture parameters always come from
-``seed``, so queries are held-out draws from the same mixture.
+``seed``, so queries are held-out draws from the same mixture.  The device generators depend on
+torch's generator, so their draws are reproducible for a given torch build, not across builds.
 """
 from __future__ import annotations
 
@@ -82,4 +89,54 @@ def sign_codes(x: np.ndarray, tables: int, bits: int, seed: int = 0, center: np.
         for t in range(tables):
             side = (xc @ planes[t]) > 0
             out[t, s:s + chunk] = (side.astype(np.uint64) * weights).sum(1, dtype=np.uint64)
+    return out
+
+
+def mixture_unit_device(n: int, d: int = 960, n_comp: int = 32, block: int = 16, seed: int = 0,
+                        queries: bool = False, chunk: int = 1 << 17):
+    """``n`` x ``d`` float32 CUDA tensor in [0, 1], L1-normalised per block of ``block`` dims: a
+    Dirichlet-weighted mixture of ``n_comp`` gamma-distributed components, drawn on the GPU."""
+    import torch
+    assert d % block == 0
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    # component parameters always from `seed`; samples from seed + 1 for queries
+    weights = torch._sample_dirichlet(torch.full((n_comp,), 5.0, device="cuda"), generator=g)
+    alpha = torch._standard_gamma(torch.full((n_comp, d), 2.0, device="cuda"), generator=g) + 0.05
+    gs = torch.Generator(device="cuda").manual_seed(seed + 1) if queries else g
+    out = torch.empty((n, d), dtype=torch.float32, device="cuda")
+    for s0 in range(0, n, chunk):
+        e = min(n, s0 + chunk)
+        comp = torch.multinomial(weights, e - s0, replacement=True, generator=gs)
+        x = torch._standard_gamma(alpha[comp], generator=gs).view(e - s0, d // block, block)
+        x /= x.sum(dim=2, keepdim=True)
+        out[s0:e] = x.view(e - s0, d)
+    return out
+
+
+def mixture_aniso_device(n: int, d: int = 96, n_comp: int = 1024, seed: int = 0, queries: bool = False,
+                         spread: float = 10.0, decay: float = 0.7):
+    """``n`` x ``d`` float32 CUDA tensor from a seeded mixture of ``n_comp`` anisotropic Gaussians:
+    centres ~ N(0, spread^2 I); component k draws R_k (s * z) with R_k a random rotation (QR of a
+    Gaussian matrix) and the spectrum s_i = (i + 1)^-decay scaled by a per-component U(0.5, 1.5)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    weights = torch._sample_dirichlet(torch.full((n_comp,), 5.0, device="cuda"), generator=g)
+    centres = torch.randn((n_comp, d), generator=g, device="cuda") * spread
+    q, r = torch.linalg.qr(torch.randn((n_comp, d, d), generator=g, device="cuda"))
+    q = q * torch.sign(torch.diagonal(r, dim1=1, dim2=2)).unsqueeze(1)  # uniformly random orthogonal
+    spec = (torch.arange(1, d + 1, device="cuda", dtype=torch.float32) ** -decay)
+    scale = torch.rand((n_comp, 1), generator=g, device="cuda") + 0.5
+    basis = q * (spec.unsqueeze(0) * scale).unsqueeze(1)  # R_k diag(s_k)
+    gs = torch.Generator(device="cuda").manual_seed(seed + 1) if queries else g
+    comp = torch.cat([torch.multinomial(weights, min(1 << 20, n - s0), replacement=True, generator=gs)
+                      for s0 in range(0, n, 1 << 20)])
+    order = torch.argsort(comp, stable=True)
+    counts = torch.bincount(comp, minlength=n_comp).tolist()
+    z = torch.randn((n, d), generator=gs, device="cuda")  # row i of z belongs to the i-th row in component order
+    out = torch.empty((n, d), dtype=torch.float32, device="cuda")
+    start = 0
+    for k, c in enumerate(counts):  # one rotation per component: a matmul over its rows
+        if c:
+            out[order[start:start + c]] = centres[k] + z[start:start + c] @ basis[k].T
+        start += c
     return out

@@ -9,6 +9,11 @@
         the base above the L2 size).  --phase-clocks runs the same searches on the diagnostic
         build of the library (EFG_PHASE_CLOCKS: every CTA of nnexp_kernel reports the SM cycles
         of each phase) and prints each search's phase shares after its line.
+    python -m efanna_gb300.profiling build [--n N] [--dim D] [--data u8|unit|aniso] [--K K] [--L L]
+                                           [--check C] [--S S] [--trees T] [--ml M] [--iter I]
+        builds the graph of one configuration from host data (the base drawn on the GPU for the
+        unit and aniso generators and copied back) and reports the build's phases and the graph
+        recall@K of 2000 sampled rows against their exact neighbours.
     python -m efanna_gb300.profiling knn [--n N] [--nq Q] [--dim D] [--k K] [--data u8|unit]
                                          [--screening auto|fp32|split] [--repeat R]
         times the exact k-NN (tensor-core or FP32 screening) on seeded data: per call the
@@ -107,6 +112,50 @@ def knn_case(n: int, nq: int, dim: int, k: int, data: str, screening: str, repea
                  st.stages, st.nchunks, st.ctas))
 
 
+def make_base(n: int, dim: int, data: str, seed: int = 0, queries: bool = False):
+    """Host float32 rows of one of the seeded generators."""
+    from efanna_gb300 import datasets
+    if data == "u8":
+        return datasets.mixture_u8(n, dim, seed=seed, queries=queries)
+    if data == "unit":
+        return datasets.mixture_unit_device(n, dim, seed=seed, queries=queries).cpu().numpy()
+    return datasets.mixture_aniso_device(n, dim, seed=seed, queries=queries).cpu().numpy()
+
+
+def build_case(n: int, dim: int, data: str, K: int, L: int, check: int, S: int, trees: int, ml: int,
+               iters: int) -> None:
+    import time
+
+    import torch
+
+    import efanna_gb300 as E
+    t0 = time.perf_counter()
+    x = make_base(n, dim, data)
+    gen_s = time.perf_counter() - t0
+    idx = E.Index(x, E.IndexParams(trees=trees, merge_level=ml, epochs=iters, check=check, L=L, K=K, S=S))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx.build_index()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    st = idx.build_stats()
+    g = idx.graph()
+    rows = np.sort(np.random.default_rng(3).choice(n, min(n, 2000), replace=False))
+    X = torch.from_numpy(x).cuda()
+    S_ = X[torch.from_numpy(rows).cuda()].contiguous()
+    gt = torch.zeros((len(rows), K + 1), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), n, dim, dim, S_.data_ptr(), len(rows), dim, K + 1, gt.data_ptr())
+    torch.cuda.synchronize()
+    gtn = gt.cpu().numpy()
+    # the sampled rows are base rows: each one's exact K neighbours other than itself
+    rec = np.mean([len(set(g[r].tolist()) & set([v for v in gtn[i] if v != r][:K])) / K for i, r in enumerate(rows)])
+    print("build %s %d x %d K=%d L=%d check=%d S=%d trees=%d ml=%d iter=%d: data %.1f s, build %.3f s (trees %.1f ms, "
+          "init %.1f ms, refine %.1f ms), join pairs %d, records %d; graph recall@%d (2000 rows) %.4f"
+          % (data, n, dim, K, L, check, S, trees, ml, iters, gen_s, build_s, st.trees_ms, st.init_ms, st.refine_ms,
+             st.join_pairs, st.join_records, K, rec), flush=True)
+    idx.close()
+
+
 def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2,
                 method: int = 0, recall: bool = False) -> None:
     import time
@@ -203,6 +252,17 @@ if __name__ == "__main__":
     s.add_argument("--recall", action="store_true", help="also report recall@10 against the exact 10-NN")
     s.add_argument("--phase-clocks", action="store_true",
                    help="run on the diagnostic build and print per-phase cycle shares of nnexp_kernel")
+    b = sub.add_parser("build")
+    b.add_argument("--n", type=int, default=1000000)
+    b.add_argument("--dim", type=int, default=128)
+    b.add_argument("--data", default="u8", choices=["u8", "unit", "aniso"])
+    b.add_argument("--K", type=int, default=10)
+    b.add_argument("--L", type=int, default=30)
+    b.add_argument("--check", type=int, default=25)
+    b.add_argument("--S", type=int, default=10)
+    b.add_argument("--trees", type=int, default=8)
+    b.add_argument("--ml", type=int, default=8)
+    b.add_argument("--iter", type=int, default=8)
     kn = sub.add_parser("knn")
     kn.add_argument("--n", type=int, default=1000000)
     kn.add_argument("--nq", type=int, default=10000)
@@ -212,7 +272,9 @@ if __name__ == "__main__":
     kn.add_argument("--screening", default="auto", choices=["auto", "fp32", "split"])
     kn.add_argument("--repeat", type=int, default=3)
     a = ap.parse_args()
-    if a.cmd == "knn":
+    if a.cmd == "build":
+        build_case(a.n, a.dim, a.data, a.K, a.L, a.check, a.S, a.trees, a.ml, a.iter)
+    elif a.cmd == "knn":
         knn_case(a.n, a.nq, a.dim, a.k, a.data, a.screening, a.repeat)
     elif a.cmd == "table":
         print(launch_table(a.csv))

@@ -195,6 +195,8 @@ def run_gpu(args):
     Q = torch.from_numpy(q).to(dev)
     gt = torch.zeros((nq, 10), dtype=torch.int32, device=dev)
     E.brute_force_knn_device(X.data_ptr(), args.n, 128, 128, Q.data_ptr(), nq, 128, 10, gt.data_ptr())
+    torch.cuda.synchronize()
+    gt_knn = knn_line(E.knn_stats(), "BF16 (exact on byte-valued data)")
     samp = np.random.default_rng(0).choice(args.n, min(args.n, 10000), replace=False)
     S = X[torch.from_numpy(samp).to(dev)].contiguous()
     gt11 = torch.zeros((len(samp), 11), dtype=torch.int32, device=dev)
@@ -365,6 +367,11 @@ def run_gpu(args):
         idx.close()
         idx = None
         line["batching"] = measure_batching(E, X, args)
+    line["exact_knn"] = gt_knn
+    if not args.no_config1:
+        line["config1"] = measure_config1(E)
+    if not args.no_p960:
+        line["precision_960"] = measure_precision_960(E, args, hbm, peak_kind)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if idx is not None:
@@ -581,6 +588,174 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
                    "clusters (8 seeds each) and a rung per query; BF16 screening, FP32 re-rank"}
     L.close()
     return res
+
+
+# the precision form's workload: 1M x 960 unit-block vectors, K = 100 graph
+P960_GRAPH = dict(trees=8, merge_level=8, epochs=8, check=200, L=200, K=100, S=10)
+P960_LADDER = [(4, 1200, 200), (4, 2000, 300), (4, 3000, 400), (6, 4000, 500), (8, 6000, 700), (8, 8000, 1000)]
+
+
+def measure_precision_960(E, args, hbm, peak_kind):
+    """BASELINE's high-dimensional precision workload: N x 960 vectors of the unit-block generator
+    (values in [0, 1], L1-normalised blocks of 16; drawn on the GPU), a K = 100 graph (trees 8,
+    ml 8, iter 8, L 200, check 200, S 10) searched with its own 8 trees; 10k held-out queries,
+    k = 100.  Reports the build, recall@100 of FP32, BF16 and FP8 screening (FP32 re-rank) against
+    the exact 100-NN at the first ladder setting where FP32 reaches 0.95, the screened distances'
+    error against FP64, and device-timed queries/s with the HBM roofline per precision."""
+    import torch
+    from efanna_gb300 import datasets
+    n, d, nq, k = args.n, 960, args.nq, 100
+    t0 = time.perf_counter()
+    X = datasets.mixture_unit_device(n, d, seed=0)
+    Q = datasets.mixture_unit_device(nq, d, seed=0, queries=True)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    idx = E.Index.from_device(X.data_ptr(), n, d, d, E.IndexParams(**P960_GRAPH))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx.build_index()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    bst = idx.build_stats()
+    # exact 100-NN of the queries (tensor-core screening, hi + lo split on this float data)
+    gt = torch.zeros((nq, k), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), n, d, d, Q.data_ptr(), nq, d, k, gt.data_ptr())
+    torch.cuda.synchronize()
+    kst = E.knn_stats()
+    gt = gt.cpu().numpy()
+    # graph recall@100 of 1000 sampled rows
+    rows = np.sort(np.random.default_rng(2).choice(n, 1000, replace=False))
+    R = X[torch.from_numpy(rows).cuda()].contiguous()
+    g101 = torch.zeros((len(rows), k + 1), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), n, d, d, R.data_ptr(), len(rows), d, k + 1, g101.data_ptr())
+    torch.cuda.synchronize()
+    g101 = g101.cpu().numpy()
+    graph = idx.graph()
+    graph_recall = float(np.mean([len(set(graph[r].tolist()) & set([v for v in g101[i] if v != r][:k])) / k
+                                  for i, r in enumerate(rows)]))
+    out = torch.zeros((nq, k), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def run(pt, prec):
+        idx.set_search_precision(prec)
+        idx.set_search_params(pt[0], pt[1], pt[2], 8)
+        idx.knn_search_device(k, Q.data_ptr(), nq, d, out.data_ptr(), stream.cuda_stream)
+
+    def rec_of():
+        torch.cuda.synchronize()
+        r = out.cpu().numpy()
+        return float(np.mean([len(set(a.tolist()) & set(b.tolist())) / k for a, b in zip(r, gt)]))
+
+    ladder, point = [], None
+    for pt in P960_LADDER:
+        run(pt, "fp32")
+        rc = rec_of()
+        ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@100": round(rc, 4)})
+        if rc >= TARGET:
+            point = pt
+            break
+    point = point or P960_LADDER[-1]
+    # screened distances against FP64: 64 queries x 256 random base rows
+    rng = np.random.default_rng(0)
+    ids = rng.integers(0, n, (64, 256)).astype(np.uint32)
+    I = torch.from_numpy(ids.view(np.int32)).cuda()
+    q64 = Q[:64].double().cpu().numpy()
+    x64 = X[torch.from_numpy(ids.reshape(-1).astype(np.int64)).cuda()].double().cpu().numpy().reshape(64, 256, d)
+    ref = ((x64 - q64[:, None, :]) ** 2).sum(-1)
+    per = {}
+    for prec in ("fp32", "bf16", "fp8"):
+        dd = torch.zeros((64, 256), dtype=torch.float32, device="cuda")
+        idx.screen_distances_device(prec, Q.data_ptr(), 64, d, I.data_ptr(), 256, dd.data_ptr())
+        torch.cuda.synchronize()
+        rel = np.abs(dd.cpu().numpy().astype(np.float64) - ref) / np.maximum(ref, 1e-30)
+        run(point, prec)
+        rc = rec_of()
+        res_host = None
+        idx.set_search_precision(prec)
+        idx.set_search_params(point[0], point[1], point[2], 8)
+        res_host = idx.knn_search(k, Q[:1000].cpu().numpy())
+        st = idx.search_stats()
+        evq, exq = st.distance_evals / 1000, st.expanded_nodes / 1000
+        row_b = {"fp32": d * 4, "bf16": d * 2, "fp8": d + 4}[prec]
+        bytes_q = evq * row_b + exq * P960_GRAPH["K"] * 4 + point[1] * 4 + d * 4 + st.reranked * d * 4
+        for _ in range(args.warmup):
+            run(point, prec)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            run(point, prec)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        achieved = bytes_q * nq / (ms / 1e3) / 1e9
+        per[prec] = {"recall@100": round(rc, 4), "value": round(nq / (ms / 1e3), 1), "unit": "queries/s",
+                     "ms_per_step": round(ms, 4),
+                     "distance_error_vs_fp64": {"max_rel": float("%.3g" % rel.max()),
+                                                "mean_rel": float("%.3g" % rel.mean())},
+                     "roofline": {"bound": "hbm", "kernel": "nnexp_kernel", "achieved": round(achieved, 1),
+                                  "peak": hbm, "peak_kind": peak_kind + " (burst)", "unit": "GB/s",
+                                  "frac": round(achieved / hbm, 4), "algorithmic_bytes_per_query": round(bytes_q, 1),
+                                  "distance_evals_per_query": round(evq, 1)}}
+        del res_host
+    idx.set_search_precision("fp32")
+    idx.close()
+    return {"workload": "%s x 960 unit-block vectors (drawn on the GPU), K=100 graph (trees 8, ml 8, iter 8, L 200, "
+                        "check 200, S 10), 8 search trees, %d queries, k=100" % (workload_size(n), nq),
+            "data_s": round(gen_s, 2), "graph_build_s": round(build_s, 3),
+            "build_phases_ms": {"trees": round(bst.trees_ms, 1), "init": round(bst.init_ms, 1),
+                                "refine": round(bst.refine_ms, 1)},
+            "join_pairs": int(bst.join_pairs), "graph_recall@100": round(graph_recall, 4),
+            "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2]}, "ladder": ladder,
+            "exact_knn": knn_line(kst, "hi + lo BF16 split (3 products per value)"),
+            **per}
+
+
+def measure_config1(E):
+    """The CPU-runnable configuration: N = 100,000 x 128 of the byte-valued mixture, graph (trees,
+    ml, iter, L, check, K, S) = (8, 8, 8, 30, 25, 10, 10) built from host rows; graph recall@10 of
+    every row against its exact 10-NN, beside the reference's three 8-thread builds recorded in
+    tests/golden/ref_recall_100k.json (parity window 0.005)."""
+    import torch
+    from efanna_gb300 import datasets
+    x = datasets.mixture_u8(100_000, 128, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = E.Index(x, E.IndexParams(**GRAPH))
+    idx.build_index()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    X = torch.from_numpy(x).cuda()
+    gt = torch.zeros((100_000, 10), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), 100_000, 128, 128, X.data_ptr(), 100_000, 128, 10, gt.data_ptr(),
+                             exclude_self=True)
+    torch.cuda.synchronize()
+    rec = recall(idx.graph(), gt.cpu().numpy())
+    idx.close()
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "ref_recall_100k.json")))
+    multi = [r["recall_at_10"] for r in ref["runs"] if r["threads"] > 1]
+    return {"workload": "100k x 128 FP32, K=10 graph (trees 8, ml 8, iter 8, L 30, check 25, S 10)",
+            "graph_build_s": round(build_s, 4), "graph_build_input": "host rows (copy to the device included)",
+            "graph_recall@10": round(rec, 5), "reference_recall@10_8threads": multi,
+            "reference_mean": round(float(np.mean(multi)), 5), "within_0.005": bool(abs(rec - np.mean(multi)) <= 0.005)}
+
+
+def knn_line(kst, form):
+    """The exact k-NN call's timings and its screening kernel's tensor roofline."""
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = float(json.load(open(pk))["bf16_tflops"]) if os.path.exists(pk) else 1900.0
+    tf = kst.screen_flops / (kst.screen_ms * 1e-3) / 1e12 if kst.screen_ms else 0.0
+    ti = kst.tile_flops / (kst.screen_ms * 1e-3) / 1e12 if kst.screen_ms else 0.0
+    return {"kernel": "tc_knn_kernel", "form": form, "convert_ms": round(kst.convert_ms, 3),
+            "bound_ms": round(kst.bound_ms, 3), "screen_ms": round(kst.screen_ms, 3),
+            "merge_ms": round(kst.merge_ms, 3),
+            "roofline": {"bound": "tensor", "achieved": round(tf, 1), "issued": round(ti, 1), "peak": peak,
+                         "peak_kind": ("measured" if os.path.exists(pk) else "fallback") + " (burst, bf16 dense)",
+                         "unit": "TFLOP/s", "frac": round(tf / peak, 4), "frac_issued": round(ti / peak, 4)}}
+
+
+def workload_size(v):
+    return "%gM" % (v / 1e6) if v % 1_000_000 == 0 else "%gk" % (v / 1e3) if v % 1000 == 0 else str(v)
 
 
 # kgraph search (search method 1) settings in ascending cost
@@ -825,6 +1000,8 @@ def main():
     ap.add_argument("--no-wide", action="store_true", help="skip the 48-tree measurement")
     ap.add_argument("--no-hashing", action="store_true", help="skip the hashing-seeded search")
     ap.add_argument("--no-kgraph", action="store_true", help="skip the kgraph search (method 1)")
+    ap.add_argument("--no-p960", action="store_true", help="skip the 1M x 960 precision workload")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 100k build and its recall parity")
     ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--in-flight", type=int, default=4, help="batches in flight in the batching form")
     ap.add_argument("--train-queries", type=int, default=50_000)

@@ -159,3 +159,33 @@ def test_screened_search_recall_at_100(efg):
     print("recall@100: fp32 %.4f bf16 %.4f fp8 %.4f" % (rec["fp32"], rec["bf16"], rec["fp8"]))
     assert rec["bf16"] >= rec["fp32"] - 0.01
     assert rec["fp8"] >= rec["fp32"] - 0.03
+
+
+def test_precision_workload_at_100k(efg):
+    """The 960-d precision workload at N = 100,000 (unit-block generator, drawn on the GPU): K = 100
+    graph (trees 8, ml 8, iter 8, L 200, check 200, S 10), 500 held-out queries, k = 100.  BF16
+    screening with the FP32 re-rank keeps recall@100 within 0.005 of the FP32 search; FP8 within 0.03."""
+    n, d, nq = 100_000, 960, 500
+    X = datasets.mixture_unit_device(n, d, seed=5)
+    Q = datasets.mixture_unit_device(nq, d, seed=5, queries=True)
+    gt = torch.zeros((nq, 100), dtype=torch.int32, device="cuda")
+    efg.brute_force_knn_device(X.data_ptr(), n, d, d, Q.data_ptr(), nq, d, 100, gt.data_ptr())
+    torch.cuda.synchronize()
+    gt = gt.cpu().numpy()
+    idx = efg.Index.from_device(X.data_ptr(), n, d, d,
+                                efg.IndexParams(trees=8, merge_level=8, epochs=8, check=200, L=200, K=100, S=10))
+    idx.build_index()
+    idx.set_search_params(4, 2000, 300, 8)
+    out = torch.zeros((nq, 100), dtype=torch.int32, device="cuda")
+    rec = {}
+    for prec in ("fp32", "bf16", "fp8"):
+        idx.set_search_precision(prec)
+        idx.knn_search_device(100, Q.data_ptr(), nq, d, out.data_ptr())
+        torch.cuda.synchronize()
+        res = out.cpu().numpy()
+        rec[prec] = np.mean([len(set(r.tolist()) & set(g.tolist())) / 100 for r, g in zip(res, gt)])
+    print("N=100k d=960 recall@100: fp32 %.4f bf16 %.4f fp8 %.4f" % (rec["fp32"], rec["bf16"], rec["fp8"]))
+    assert rec["fp32"] > 0.9
+    assert rec["bf16"] >= rec["fp32"] - 0.005
+    assert rec["fp8"] >= rec["fp32"] - 0.03
+    idx.close()

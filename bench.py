@@ -592,7 +592,9 @@ def measure_learned(E, idx, X, Q, q, gt, nq, stream, ws, args, rungs=None):
 
 # the precision form's workload: 1M x 960 unit-block vectors, K = 100 graph
 P960_GRAPH = dict(trees=8, merge_level=8, epochs=8, check=200, L=200, K=100, S=10)
-P960_LADDER = [(4, 1200, 200), (4, 2000, 300), (4, 3000, 400), (6, 4000, 500), (8, 6000, 700), (8, 8000, 1000)]
+# extend x degree candidates per epoch sit in shared memory: with degree 100, extend stays <= 300
+P960_LADDER = [(4, 1200, 200), (4, 2000, 300), (6, 3000, 300), (8, 4000, 300), (12, 6000, 300), (16, 8000, 300),
+               (24, 12000, 300)]
 
 
 def measure_precision_960(E, args, hbm, peak_kind):
@@ -648,13 +650,17 @@ def measure_precision_960(E, args, hbm, peak_kind):
 
     ladder, point = [], None
     for pt in P960_LADDER:
-        run(pt, "fp32")
+        try:
+            run(pt, "fp32")
+        except E.EfannaError as e:  # a setting whose per-query state does not fit
+            ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "error": str(e)[:80]})
+            continue
         rc = rec_of()
         ladder.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@100": round(rc, 4)})
         if rc >= TARGET:
             point = pt
             break
-    point = point or P960_LADDER[-1]
+    point = point or tuple(next((r["epochs"], r["pool"], r["extend"]) for r in reversed(ladder) if "error" not in r))
     # screened distances against FP64: 64 queries x 256 random base rows
     rng = np.random.default_rng(0)
     ids = rng.integers(0, n, (64, 256)).astype(np.uint32)

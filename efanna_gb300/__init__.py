@@ -62,7 +62,8 @@ class LearnedParams(C.Structure):
     _fields_ = [("clusters", C.c_uint32), ("kmeans_iters", C.c_uint32), ("kmeans_sample", C.c_uint32),
                 ("entries_per_cluster", C.c_uint32), ("entry_clusters", C.c_uint32), ("hidden", C.c_uint32),
                 ("rungs", C.c_uint32), ("rung", QueryParams * MAX_RUNGS), ("target", C.c_float),
-                ("train_epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64)]
+                ("train_epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64),
+                ("trace_reference", QueryParams)]
 
 
 class LearnedStats(C.Structure):
@@ -452,13 +453,16 @@ class Learned:
 
     def __init__(self, index: "Index", clusters=1024, entries_per_cluster=16, entry_clusters=8, hidden=256,
                  rungs=None, target=0.9, train_epochs=8, batch=1024, lr=1e-3, kmeans_iters=10,
-                 kmeans_sample=100000, seed=1998):
+                 kmeans_sample=100000, seed=1998, trace_reference=None):
         p = LearnedParams()
         lib().efg_learned_default_params(C.byref(p))
         p.clusters, p.entries_per_cluster, p.entry_clusters, p.hidden = clusters, entries_per_cluster, \
             entry_clusters, hidden
         p.target, p.train_epochs, p.batch, p.lr = target, train_epochs, batch, lr
         p.kmeans_iters, p.kmeans_sample, p.seed = kmeans_iters, kmeans_sample, seed
+        if trace_reference is not None:  # (epochs, pool, extend): traces scored against that plain search
+            p.trace_reference = QueryParams(int(trace_reference[0]), int(trace_reference[1]),
+                                            int(trace_reference[2]), 10)
         if rungs is not None:
             p.rungs = len(rungs)
             for i, r in enumerate(rungs):

@@ -8,7 +8,8 @@
 //      (k = 1 against the centroids), updates by one CTA per cluster summing its members in sample
 //      order (deterministic).  Then every base row is assigned, and each cluster keeps its
 //      `entries_per_cluster` members nearest the centroid, ordered by (dist, id).
-//   2. Traces (efg_learned_train): exact 10-NN of the training queries -> clusters of the true
+//   2. Traces (efg_learned_train): exact 10-NN of the training queries (or the plain search's ids at a
+//      high reference setting, for large training sets) -> clusters of those
 //      neighbours (the entry head's target distribution); plain searches at every setting of the
 //      rung ladder -> per-query recall -> the smallest setting reaching min(target, best recall)
 //      (the early-stop head's label).
@@ -687,10 +688,16 @@ int efg_learned_train(efg_learned* L, const float* d_q, uint64_t n, uint64_t row
   EFG_TRY(L->tclusters.reserve(n * GT_K));
   EFG_TRY(L->tlabel.reserve(n));
   L->ntrain = n;
-  for (uint64_t q0 = 0; q0 < n; q0 += 65536) {
-    uint64_t m = std::min<uint64_t>(n - q0, 65536);
-    EFG_TRY(exact_knn(idx->d_base, idx->n, dim, ld, L->trainq.p + q0 * ld, m, ld, GT_K, 0, 0, gt.p + q0 * GT_K,
-                            gtd.p + q0 * GT_K, s));
+  if (L->p.trace_reference.init_num > 0) {  // the plain search at a high setting stands in for the exact 10-NN
+    efg_query_params ref = L->p.trace_reference;
+    ref.k = GT_K;
+    EFG_TRY(search_device_ex(idx, L->trainq.p, n, ld, ref, nullptr, nullptr, gt.p, s, false));
+  } else {
+    for (uint64_t q0 = 0; q0 < n; q0 += 65536) {
+      uint64_t m = std::min<uint64_t>(n - q0, 65536);
+      EFG_TRY(exact_knn(idx->d_base, idx->n, dim, ld, L->trainq.p + q0 * ld, m, ld, GT_K, 0, 0, gt.p + q0 * GT_K,
+                        gtd.p + q0 * GT_K, s));
+    }
   }
   trace_clusters_kernel<<<1024, 256, 0, s>>>(gt.p, n, L->assign.p, L->tclusters.p);
   for (uint32_t r = 0; r < R; ++r) {

@@ -114,10 +114,12 @@ def mixture_unit_device(n: int, d: int = 960, n_comp: int = 32, block: int = 16,
 
 
 def mixture_aniso_device(n: int, d: int = 96, n_comp: int = 1024, seed: int = 0, queries: bool = False,
-                         spread: float = 10.0, decay: float = 0.7):
+                         spread: float = 10.0, decay: float = 0.7, sample_seed: int | None = None):
     """``n`` x ``d`` float32 CUDA tensor from a seeded mixture of ``n_comp`` anisotropic Gaussians:
     centres ~ N(0, spread^2 I); component k draws R_k (s * z) with R_k a random rotation (QR of a
-    Gaussian matrix) and the spectrum s_i = (i + 1)^-decay scaled by a per-component U(0.5, 1.5)."""
+    Gaussian matrix) and the spectrum s_i = (i + 1)^-decay scaled by a per-component U(0.5, 1.5).
+    With ``sample_seed`` the draws come from that seed (a further held-out sample, e.g. training
+    queries)."""
     import torch
     g = torch.Generator(device="cuda").manual_seed(seed)
     weights = torch._sample_dirichlet(torch.full((n_comp,), 5.0, device="cuda"), generator=g)
@@ -127,7 +129,10 @@ def mixture_aniso_device(n: int, d: int = 96, n_comp: int = 1024, seed: int = 0,
     spec = (torch.arange(1, d + 1, device="cuda", dtype=torch.float32) ** -decay)
     scale = torch.rand((n_comp, 1), generator=g, device="cuda") + 0.5
     basis = q * (spec.unsqueeze(0) * scale).unsqueeze(1)  # R_k diag(s_k)
-    gs = torch.Generator(device="cuda").manual_seed(seed + 1) if queries else g
+    if sample_seed is not None:
+        gs = torch.Generator(device="cuda").manual_seed(sample_seed)
+    else:
+        gs = torch.Generator(device="cuda").manual_seed(seed + 1) if queries else g
     comp = torch.cat([torch.multinomial(weights, min(1 << 20, n - s0), replacement=True, generator=gs)
                       for s0 in range(0, n, 1 << 20)])
     order = torch.argsort(comp, stable=True)

@@ -195,6 +195,10 @@ typedef struct efg_learned_params {
   uint32_t batch;                /* training batch                                              */
   float lr;                      /* Adam step                                                   */
   uint64_t seed;
+  /* Neighbours the traces score the rungs against: the exact 10-NN of each training query when
+   * trace_reference.init_num is 0 (the default), else the plain search's 10 ids at this setting
+   * (epochs, pool, extend; k ignored) -- for training sets whose exact neighbours cost too much. */
+  efg_query_params trace_reference;
 } efg_learned_params;
 typedef struct efg_learned_stats {
   uint64_t train_queries;

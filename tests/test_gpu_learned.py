@@ -126,3 +126,63 @@ def test_training_on_traces_and_learned_search(efg, small):
               "(rungs %s)" % (bias, cov, recall(res), mean_pool, at_cost, ["%.4f" % v for v in plain]))
         assert recall(res) >= at_cost - 0.01
     L.close()
+
+
+RUNGS5 = [(4, 400, 40), (4, 1000, 100), (4, 1500, 150), (4, 2000, 200), (4, 3000, 300), (6, 4000, 400),
+          (8, 6000, 600)]
+
+
+def test_learned_search_gains_over_plain_on_anisotropic_mixture(efg):
+    """What the trained network gains: on the learned form's data family (the anisotropic
+    1024-component mixture, d = 96; here N = 300,000 with a K = 32 graph and 100,000 training
+    traces), the learned search reaches a recall the plain search needs a larger pool for.  For the
+    coverage settings that reach recall 0.93, its mean pool size is at most 0.9 x the pool the plain
+    search needs for the same recall (interpolated along the plain ladder), on 4,000 held-out
+    queries judged by the exact 10-NN."""
+    n, d, nq = 300_000, 96, 4000
+    X = datasets.mixture_aniso_device(n, d, seed=3)
+    Q = datasets.mixture_aniso_device(nq, d, seed=3, queries=True)
+    T = datasets.mixture_aniso_device(100_000, d, seed=3, sample_seed=99)
+    idx = efg.Index.from_device(X.data_ptr(), n, d, d,
+                                efg.IndexParams(trees=8, merge_level=8, epochs=8, check=40, L=40, K=32, S=10))
+    idx.build_index()
+    idx.build_trees(16)
+    gt = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+    efg.brute_force_knn_device(X.data_ptr(), n, d, d, Q.data_ptr(), nq, d, 10, gt.data_ptr())
+    torch.cuda.synchronize()
+    gtn = gt.cpu().numpy()
+    out = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+
+    def recall():
+        torch.cuda.synchronize()
+        return np.mean([len(set(a) & set(g)) / 10 for a, g in zip(out.cpu().numpy().tolist(), gtn.tolist())])
+
+    idx.set_search_precision("bf16")
+    plain = []
+    for e, pool, ext in RUNGS5:
+        idx.set_search_params(e, pool, ext, 16)
+        idx.knn_search_device(10, Q.data_ptr(), nq, d, out.data_ptr())
+        plain.append(recall())
+    pools = [r[1] for r in RUNGS5]
+    assert all(b >= a - 0.005 for a, b in zip(plain, plain[1:]))
+    L = efg.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=RUNGS5,
+                    target=0.95, train_epochs=6, batch=1024, lr=1e-3)
+    L.train_device(T.data_ptr(), 100_000, d)
+    rung = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    cl = torch.zeros((nq, 8), dtype=torch.int32, device="cuda")
+    gains = []
+    for cov in (0.7, 0.8, 0.9, 0.95):
+        L.search_device(Q.data_ptr(), nq, d, 10, out.data_ptr(), coverage=cov)
+        rec = recall()
+        L.predict_device(Q.data_ptr(), nq, d, cl.data_ptr(), rung.data_ptr(), coverage=cov)
+        torch.cuda.synchronize()
+        mean_pool = float(np.mean([pools[i] for i in rung.cpu().numpy()]))
+        # the plain search's pool for the same recall (recall rises with the pool along the ladder)
+        need = float(np.interp(rec, plain, pools)) if plain[0] <= rec <= plain[-1] else float("nan")
+        print("coverage %.2f: learned recall %.4f at mean pool %.0f; plain needs pool %.0f (plain ladder %s)"
+              % (cov, rec, mean_pool, need, ["%.4f" % v for v in plain]))
+        if rec >= 0.93 and need == need:
+            gains.append(mean_pool / need)
+    assert gains and max(gains) <= 0.9, gains
+    L.close()
+    idx.close()

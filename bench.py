@@ -372,6 +372,8 @@ def run_gpu(args):
         line["config1"] = measure_config1(E)
     if not args.no_p960:
         line["precision_960"] = measure_precision_960(E, args, hbm, peak_kind)
+    if not args.no_c5:
+        line["learned_aniso"] = measure_learned_aniso(E, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if idx is not None:
@@ -717,6 +719,123 @@ def measure_precision_960(E, args, hbm, peak_kind):
             **per}
 
 
+# the learned form's workload: 10M x 96 anisotropic mixture, K = 32 graph
+C5_GRAPH = dict(trees=8, merge_level=8, epochs=8, check=40, L=40, K=32, S=10)
+C5_RUNGS = [(4, 400, 40), (4, 1000, 100), (4, 1500, 150), (4, 2000, 200), (4, 3000, 300), (6, 4000, 400),
+            (8, 6000, 600), (8, 8000, 800), (12, 12000, 800)]
+C5_REFERENCE = (16, 16000, 800)  # the plain search the traces' rungs are scored against
+
+
+def measure_learned_aniso(E, args):
+    """BASELINE's learned-form workload: N = 10M x 96 from the seeded anisotropic 1,024-component
+    mixture (drawn on the GPU), a K = 32 graph (trees 8, ml 8, iter 8, L 40, check 40, S 10) and 16
+    search trees; 100k held-out test queries (recall judged on the first 2,000 by the exact
+    10-NN), k = 10.  The plain BF16 search along a ladder of settings, then the learned form: k-means
+    entry clusters and the MLP (96-256-256-(1024 clusters + rungs), BF16 weights, FP32 accumulation)
+    trained on 2M traces of the plain search (their rungs scored against the plain search at a high
+    reference setting), searched at several coverages.  Device-timed queries/s (prediction included
+    for the learned search) and the gain at equal recall."""
+    import torch
+    from efanna_gb300 import datasets
+    n, d, nq, ng, ntr = args.c5_n, 96, args.c5_queries, 2000, args.c5_train
+    t0 = time.perf_counter()
+    X = datasets.mixture_aniso_device(n, d, seed=0)
+    Q = datasets.mixture_aniso_device(nq, d, seed=0, queries=True)
+    T = datasets.mixture_aniso_device(ntr, d, seed=0, sample_seed=4242)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    idx = E.Index.from_device(X.data_ptr(), n, d, d, E.IndexParams(**C5_GRAPH))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx.build_index()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    idx.build_trees(16)
+    gt = torch.zeros((ng, 10), dtype=torch.int32, device="cuda")
+    E.brute_force_knn_device(X.data_ptr(), n, d, d, Q.data_ptr(), ng, d, 10, gt.data_ptr())
+    torch.cuda.synchronize()
+    gt = gt.cpu().numpy()
+    out = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    reps = max(1, min(args.steps, 3))
+
+    def rec_of():
+        torch.cuda.synchronize()
+        r = out[:ng].cpu().numpy()
+        return float(np.mean([len(set(a) & set(b)) / 10 for a, b in zip(r.tolist(), gt.tolist())]))
+
+    def timed(f):
+        f()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(reps):
+            f()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return nq * reps / (ev0.elapsed_time(ev1) / 1e3)
+
+    idx.set_search_precision("bf16")
+    plain = []
+    for pt in C5_RUNGS:
+        idx.set_search_params(pt[0], pt[1], pt[2], 16)
+        f = lambda: idx.knn_search_device(10, Q.data_ptr(), nq, d, out.data_ptr(), stream.cuda_stream)
+        f()
+        rc = rec_of()
+        plain.append({"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(rc, 4),
+                      "value": round(timed(f), 1)})
+        if rc >= TARGET + 0.01:
+            break
+    t0 = time.perf_counter()
+    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=C5_RUNGS,
+                  target=TARGET, train_epochs=4, batch=1024, lr=1e-3, trace_reference=C5_REFERENCE)
+    torch.cuda.synchronize()
+    cluster_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    L.train_device(T.data_ptr(), ntr, d)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    st = L.stats()
+    rung = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    cl = torch.zeros((nq, 8), dtype=torch.int32, device="cuda")
+    learned = []
+    for cov in (0.5, 0.7, 0.8, 0.9, 0.95, 0.98):
+        f = lambda: L.search_device(Q.data_ptr(), nq, d, 10, out.data_ptr(), 0, stream.cuda_stream, cov)
+        f()
+        rc = rec_of()
+        L.predict_device(Q.data_ptr(), nq, d, cl.data_ptr(), rung.data_ptr(), stream.cuda_stream, cov)
+        torch.cuda.synchronize()
+        mean_pool = float(np.mean([C5_RUNGS[i][1] for i in rung.cpu().numpy()]))
+        learned.append({"coverage": cov, "recall@10": round(rc, 4), "mean_pool": round(mean_pool, 1),
+                        "value": round(timed(f), 1)})
+    pt_ms = timed(lambda: L.predict_device(Q.data_ptr(), nq, d, cl.data_ptr(), rung.data_ptr(), stream.cuda_stream,
+                                           0.9))
+    # the plain search's queries/s at each learned point's recall (log-linear between ladder points)
+    pr = [p["recall@10"] for p in plain]
+    for p in learned:
+        if pr[0] <= p["recall@10"] <= pr[-1]:
+            at = float(np.exp(np.interp(p["recall@10"], pr, [np.log(v["value"]) for v in plain])))
+            p["plain_at_equal_recall"] = round(at, 1)
+            p["gain"] = round(p["value"] / at, 3)
+    first = lambda rows: next((r for r in rows if r["recall@10"] >= TARGET), None)
+    L.close()
+    idx.close()
+    return {"workload": "%s x 96 anisotropic 1024-component mixture (drawn on the GPU), K=32 graph (trees 8, ml 8, "
+                        "iter 8, L 40, check 40, S 10), 16 search trees, %s test queries (recall on %d), k=10"
+                        % (workload_size(n), workload_size(nq), ng),
+            "data_s": round(gen_s, 2), "graph_build_s": round(build_s, 3), "precision": "bf16",
+            "plain": plain, "learned": learned, "plain_at_0.95": first(plain), "learned_at_0.95": first(learned),
+            "train_queries": int(st.train_queries), "trace_reference": {"epochs": C5_REFERENCE[0],
+                                                                        "pool": C5_REFERENCE[1],
+                                                                        "extend": C5_REFERENCE[2]},
+            "train_loss_first": round(st.train_loss_first, 4), "train_loss_last": round(st.train_loss_last, 4),
+            "rung_recall_vs_reference": [round(st.rung_recall[i], 4) for i in range(len(C5_RUNGS))],
+            "cluster_s": round(cluster_s, 2), "trace_and_train_s": round(train_s, 2),
+            "predict_queries_per_s": round(pt_ms, 1),
+            "form": "MLP 96-256-256-(1024 clusters + %d rungs) predicts 8 entry clusters (8 seeds each) and an "
+                    "early-stop rung per query; BF16 screening, FP32 re-rank" % len(C5_RUNGS)}
+
+
 def measure_config1(E):
     """The CPU-runnable configuration: N = 100,000 x 128 of the byte-valued mixture, graph (trees,
     ml, iter, L, check, K, S) = (8, 8, 8, 30, 25, 10, 10) built from host rows; graph recall@10 of
@@ -1008,6 +1127,10 @@ def main():
     ap.add_argument("--no-kgraph", action="store_true", help="skip the kgraph search (method 1)")
     ap.add_argument("--no-p960", action="store_true", help="skip the 1M x 960 precision workload")
     ap.add_argument("--no-config1", action="store_true", help="skip the 100k build and its recall parity")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 10M x 96 learned-form workload")
+    ap.add_argument("--c5-n", type=int, default=10_000_000)
+    ap.add_argument("--c5-queries", type=int, default=100_000)
+    ap.add_argument("--c5-train", type=int, default=2_000_000)
     ap.add_argument("--batch-queries", type=int, default=200_000)
     ap.add_argument("--in-flight", type=int, default=4, help="batches in flight in the batching form")
     ap.add_argument("--train-queries", type=int, default=50_000)

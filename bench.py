@@ -374,6 +374,13 @@ def run_gpu(args):
         line["precision_960"] = measure_precision_960(E, args, hbm, peak_kind)
     if not args.no_c5:
         line["learned_aniso"] = measure_learned_aniso(E, args)
+        # the family's harder member (spectrum decay 0.3) at 1M, where per-query difficulty varies most
+        line["learned_aniso_hard_1M"] = measure_learned_aniso(
+            E, args, n=1_000_000, decay=0.3, ntrain=200_000,
+            rungs=[(4, 400, 40), (4, 1000, 100), (4, 1500, 150), (4, 2000, 200), (4, 3000, 300), (6, 4000, 400),
+                   (8, 6000, 600)],
+            plain_ladder=[(4, 400, 40), (4, 1000, 100), (4, 1500, 150), (4, 2000, 200), (4, 3000, 300),
+                          (6, 4000, 400), (8, 6000, 600), (8, 8000, 800)], reference=(12, 12000, 800))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if idx is not None:
@@ -729,7 +736,7 @@ C5_PLAIN = C5_RUNGS + [(6, 4000, 400)]
 C5_REFERENCE = (8, 8000, 800)  # the plain search the traces' rungs are scored against
 
 
-def measure_learned_aniso(E, args):
+def measure_learned_aniso(E, args, n=None, decay=0.35, plain_ladder=None, rungs=None, reference=None, ntrain=None):
     """BASELINE's learned-form workload: N = 10M x 96 from the seeded anisotropic 1,024-component
     mixture (drawn on the GPU), a K = 32 graph (trees 8, ml 8, iter 8, L 40, check 40, S 10) and 16
     search trees; 100k held-out test queries (recall judged on the first 2,000 by the exact
@@ -740,11 +747,15 @@ def measure_learned_aniso(E, args):
     for the learned search) and the gain at equal recall."""
     import torch
     from efanna_gb300 import datasets
-    n, d, nq, ng, ntr = args.c5_n, 96, args.c5_queries, 2000, args.c5_train
+    n = n or args.c5_n
+    d, nq, ng, ntr = 96, args.c5_queries, 2000, ntrain or args.c5_train
+    rungs = rungs or C5_RUNGS
+    plain_ladder = plain_ladder or C5_PLAIN
+    reference = reference or C5_REFERENCE
     t0 = time.perf_counter()
-    X = datasets.mixture_aniso_device(n, d, seed=0)
-    Q = datasets.mixture_aniso_device(nq, d, seed=0, queries=True)
-    T = datasets.mixture_aniso_device(ntr, d, seed=0, sample_seed=4242)
+    X = datasets.mixture_aniso_device(n, d, seed=0, decay=decay)
+    Q = datasets.mixture_aniso_device(nq, d, seed=0, queries=True, decay=decay)
+    T = datasets.mixture_aniso_device(ntr, d, seed=0, sample_seed=4242, decay=decay)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     idx = E.Index.from_device(X.data_ptr(), n, d, d, E.IndexParams(**C5_GRAPH))
@@ -780,7 +791,7 @@ def measure_learned_aniso(E, args):
 
     idx.set_search_precision("bf16")
     plain = []
-    for pt in C5_PLAIN:
+    for pt in plain_ladder:
         idx.set_search_params(pt[0], pt[1], pt[2], 16)
         f = lambda: idx.knn_search_device(10, Q.data_ptr(), nq, d, out.data_ptr(), stream.cuda_stream)
         f()
@@ -790,8 +801,8 @@ def measure_learned_aniso(E, args):
         if rc >= TARGET + 0.01:
             break
     t0 = time.perf_counter()
-    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=C5_RUNGS,
-                  target=TARGET, train_epochs=4, batch=1024, lr=1e-3, trace_reference=C5_REFERENCE)
+    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256, rungs=rungs,
+                  target=TARGET, train_epochs=4, batch=1024, lr=1e-3, trace_reference=reference)
     torch.cuda.synchronize()
     cluster_s = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -808,7 +819,7 @@ def measure_learned_aniso(E, args):
         rc = rec_of()
         L.predict_device(Q.data_ptr(), nq, d, cl.data_ptr(), rung.data_ptr(), stream.cuda_stream, cov)
         torch.cuda.synchronize()
-        mean_pool = float(np.mean([C5_RUNGS[i][1] for i in rung.cpu().numpy()]))
+        mean_pool = float(np.mean([rungs[i][1] for i in rung.cpu().numpy()]))
         learned.append({"coverage": cov, "recall@10": round(rc, 4), "mean_pool": round(mean_pool, 1),
                         "value": round(timed(f), 1)})
     pt_ms = timed(lambda: L.predict_device(Q.data_ptr(), nq, d, cl.data_ptr(), rung.data_ptr(), stream.cuda_stream,
@@ -828,16 +839,16 @@ def measure_learned_aniso(E, args):
                         % (workload_size(n), workload_size(nq), ng),
             "data_s": round(gen_s, 2), "graph_build_s": round(build_s, 3), "precision": "bf16",
             "plain": plain, "learned": learned, "plain_at_0.95": first(plain), "learned_at_0.95": first(learned),
-            "train_queries": int(st.train_queries), "trace_reference": {"epochs": C5_REFERENCE[0],
-                                                                        "pool": C5_REFERENCE[1],
-                                                                        "extend": C5_REFERENCE[2]},
+            "train_queries": int(st.train_queries), "trace_reference": {"epochs": reference[0],
+                                                                        "pool": reference[1],
+                                                                        "extend": reference[2]},
             "train_loss_first": round(st.train_loss_first, 4), "train_loss_last": round(st.train_loss_last, 4),
-            "rung_recall_vs_reference": [round(st.rung_recall[i], 4) for i in range(len(C5_RUNGS))],
+            "rung_recall_vs_reference": [round(st.rung_recall[i], 4) for i in range(len(rungs))],
             "cluster_s": round(cluster_s, 2), "trace_and_train_s": round(train_s, 2),
             "predict_queries_per_s": round(pt_ms, 1),
-            "generator": "datasets.mixture_aniso_device (spread 0.3, spectrum decay 0.35), seeds 0 / 1 / 4242",
+            "generator": "datasets.mixture_aniso_device (spread 0.3, spectrum decay %g), seeds 0 / 1 / 4242" % decay,
             "form": "MLP 96-256-256-(1024 clusters + %d rungs) predicts 8 entry clusters (8 seeds each) and an "
-                    "early-stop rung per query; BF16 screening, FP32 re-rank" % len(C5_RUNGS)}
+                    "early-stop rung per query; BF16 screening, FP32 re-rank" % len(rungs)}
 
 
 def measure_config1(E):

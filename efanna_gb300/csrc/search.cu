@@ -84,6 +84,65 @@ __device__ __forceinline__ bool ht_insert(uint32_t* ht, uint32_t size, uint32_t 
   atomicOr(ovf, 1u);
   return false;
 }
+// ht_insert continued from slot h after `done` probes of id's sequence.
+__device__ __forceinline__ bool ht_insert_from(uint32_t* ht, uint32_t size, uint32_t limit, uint32_t* count,
+                                               uint32_t* ovf, uint32_t id, uint32_t h, uint32_t done) {
+  const uint32_t st = ht_step(id, size);
+  for (uint32_t probe = done; probe < size; ++probe) {
+    uint32_t cur = *reinterpret_cast<volatile const uint32_t*>(&ht[h]);
+    if (cur == kEmpty) {
+      if (*reinterpret_cast<volatile uint32_t*>(count) >= limit) {
+        atomicOr(ovf, 1u);
+        return false;
+      }
+      uint32_t prev = atomicCAS(&ht[h], kEmpty, id);
+      if (prev == kEmpty) return true;
+      cur = prev;
+    }
+    if ((cur & ID_MASK) == id) return false;
+    h = ht_next(h, st, size);
+  }
+  atomicOr(ovf, 1u);
+  return false;
+}
+
+// XR inserts of one thread with their first probes issued together: the first slots' loads, then
+// the compare-and-swaps of the ids whose first slot was empty, then (rarely) the rest of a probe
+// sequence.  The same outcome as XR ht_insert calls in order: an id met twice in the batch takes
+// its slot once (the second CAS returns the first's id).  kEmpty entries are skipped.
+template <int XR>
+__device__ __forceinline__ void ht_insert_batch(uint32_t* ht, uint32_t size, uint32_t limit, uint32_t* count,
+                                                uint32_t* ovf, const uint32_t (&id)[XR], bool (&fresh)[XR]) {
+  uint32_t h[XR], cur[XR], prev[XR];
+#pragma unroll
+  for (int u = 0; u < XR; ++u) h[u] = id[u] != kEmpty ? ht_slot(id[u], size) : 0u;
+#pragma unroll
+  for (int u = 0; u < XR; ++u) cur[u] = id[u] != kEmpty ? *reinterpret_cast<volatile const uint32_t*>(&ht[h[u]]) : 0u;
+  const bool full = *reinterpret_cast<volatile uint32_t*>(count) >= limit;
+#pragma unroll
+  for (int u = 0; u < XR; ++u)
+    prev[u] = (id[u] != kEmpty && cur[u] == kEmpty && !full) ? atomicCAS(&ht[h[u]], kEmpty, id[u]) : cur[u];
+#pragma unroll
+  for (int u = 0; u < XR; ++u) {
+    fresh[u] = false;
+    if (id[u] == kEmpty) continue;
+    uint32_t c = cur[u];
+    if (c == kEmpty) {
+      if (full) {
+        atomicOr(ovf, 1u);
+        continue;
+      }
+      if (prev[u] == kEmpty) {
+        fresh[u] = true;
+        continue;
+      }
+      c = prev[u];
+    }
+    if ((c & ID_MASK) == id[u]) continue;
+    fresh[u] = ht_insert_from(ht, size, limit, count, ovf, id[u], ht_next(h[u], ht_step(id[u], size), size), 1);
+  }
+}
+
 __device__ __forceinline__ bool ht_contains(const uint32_t* ht, uint32_t size, uint32_t id) {
   uint32_t h = ht_slot(id, size), st = ht_step(id, size);
   for (uint32_t probe = 0; probe < size; ++probe) {

@@ -418,31 +418,6 @@ __global__ void assemble_kernel(const uint32_t* __restrict__ clusters, const uin
   params[q] = p;
 }
 
-// Row i of out (ld floats: the query's dim values, zero padded) is query perm[i] of q (row_stride
-// floats apart).
-__global__ void gather_queries_kernel(const float* __restrict__ q, uint64_t row_stride, uint32_t dim,
-                                      const uint32_t* __restrict__ perm, uint64_t n, uint32_t ld,
-                                      float* __restrict__ out) {
-  const uint64_t total = n * ld;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t r = i / ld;
-    const uint32_t c = (uint32_t)(i - r * ld);
-    out[i] = c < dim ? q[(uint64_t)perm[r] * row_stride + c] : 0.f;
-  }
-}
-
-// Row i of out (w words) is row perm[i] of in (gather), or row perm[i] of out is row i of in (scatter).
-template <bool SCATTER, typename T>
-__global__ void permute_rows_kernel(const T* __restrict__ in, const uint32_t* __restrict__ perm, uint64_t n,
-                                    uint32_t w, T* __restrict__ out) {
-  const uint64_t total = n * w;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t r = i / w, c = i - r * w;
-    if (SCATTER) out[(uint64_t)perm[r] * w + c] = in[i];
-    else out[i] = in[(uint64_t)perm[r] * w + c];
-  }
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -471,10 +446,6 @@ struct efg_learned {
   DevBuf<float> h1, h2, z, dz, dh2, dh1;
   DevBuf<double> loss;
   DevBuf<uint32_t> pred_c, pred_r, seeds, batch_rows;
-  // the search's per-rung buckets: query order, queries, seeds and ids in bucket order
-  DevBuf<uint32_t> perm, bseeds;
-  DevBuf<float> bq;
-  DevBuf<int32_t> bout;
   DevBuf<efg_query_params> qp, ladder;
   efg_learned_stats stats{};
 };
@@ -803,61 +774,27 @@ int efg_learned_search_device(efg_learned* L, const float* d_q, uint64_t nq, uin
                               float coverage, int rung_bias, int32_t* d_out, void* stream) {
   if (!L || ((!d_q || !d_out) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (nq == 0) return EFG_OK;
-  if (row_stride < L->idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
-  if (nq > 0xffffffffull) return fail(EFG_ERR_ARG, "at most 2^32 - 1 queries per call");
   efg_index* idx = L->idx;
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t E = L->p.entry_clusters, m = L->p.entries_per_cluster, S = E * m;
-  for (uint32_t r = 0; r < L->R; ++r)
-    if ((int)k > L->p.rung[r].init_num) return fail(EFG_ERR_ARG, "k above a pool of the ladder");
+  const uint32_t E = L->p.entry_clusters, m = L->p.entries_per_cluster;
+  efg_query_params lim{0, 1, 0, k};
+  for (uint32_t r = 0; r < L->R; ++r) {
+    lim.epochs = std::max(lim.epochs, L->p.rung[r].epochs);
+    lim.init_num = std::max(lim.init_num, L->p.rung[r].init_num);
+    lim.extend_to = std::max(lim.extend_to, std::min(L->p.rung[r].extend_to, L->p.rung[r].init_num));
+  }
+  if ((int)k > lim.init_num) return fail(EFG_ERR_ARG, "k above the largest pool of the ladder");
   EFG_TRY(L->pred_c.reserve(std::max<uint64_t>(nq * E, 1)));
   EFG_TRY(L->pred_r.reserve(nq));
-  EFG_TRY(L->seeds.reserve(std::max<uint64_t>(nq * S, 1)));
+  EFG_TRY(L->seeds.reserve(std::max<uint64_t>(nq * E * m, 1)));
   EFG_TRY(L->qp.reserve(nq));
   EFG_TRY(efg_learned_predict_device(L, d_q, nq, row_stride, coverage, E ? L->pred_c.p : nullptr, L->pred_r.p, s));
   assemble_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(L->pred_c.p, L->pred_r.p, nq, E, L->entries.p,
                                                               std::max<uint32_t>(m, 1), m, L->ladder.p, L->R,
                                                               rung_bias, k, L->seeds.p, L->qp.p);
   EFG_CUDA(cudaGetLastError());
-  // Buckets by rung: a launch sizes every query's shared memory for its largest parameters, so each
-  // rung's queries run as one launch with that rung's own parameters.  Stable counting sort on the host.
-  std::vector<uint32_t> rung(nq), perm(nq);
-  EFG_CUDA(cudaMemcpyAsync(rung.data(), L->pred_r.p, nq * 4, cudaMemcpyDeviceToHost, s));
-  EFG_CUDA(cudaStreamSynchronize(s));
-  std::vector<uint64_t> start(L->R + 1, 0);
-  for (uint64_t i = 0; i < nq; ++i) {
-    int r = (int)rung[i] + rung_bias;
-    rung[i] = (uint32_t)(r < 0 ? 0 : (r >= (int)L->R ? (int)L->R - 1 : r));
-    ++start[rung[i] + 1];
-  }
-  for (uint32_t r = 0; r < L->R; ++r) start[r + 1] += start[r];
-  {
-    std::vector<uint64_t> pos(start.begin(), start.end() - 1);
-    for (uint64_t i = 0; i < nq; ++i) perm[pos[rung[i]]++] = (uint32_t)i;
-  }
-  const uint32_t ld = (idx->dim + 3) / 4 * 4;
-  EFG_TRY(L->perm.reserve(nq));
-  EFG_TRY(L->bq.reserve(nq * ld));
-  EFG_TRY(L->bseeds.reserve(std::max<uint64_t>(nq * S, 1)));
-  EFG_TRY(L->bout.reserve(nq * k));
-  EFG_CUDA(cudaMemcpyAsync(L->perm.p, perm.data(), nq * 4, cudaMemcpyHostToDevice, s));
-  const unsigned pg = (unsigned)std::min<uint64_t>((nq * std::max(ld, S) + 255) / 256, 152 * 16);
-  gather_queries_kernel<<<pg, 256, 0, s>>>(d_q, row_stride, idx->dim, L->perm.p, nq, ld, L->bq.p);
-  if (S) permute_rows_kernel<false, uint32_t><<<pg, 256, 0, s>>>(L->seeds.p, L->perm.p, nq, S, L->bseeds.p);
-  EFG_CUDA(cudaGetLastError());
-  for (uint32_t r = 0; r < L->R; ++r) {
-    const uint64_t c = start[r + 1] - start[r];
-    if (!c) continue;
-    efg_query_params lim = L->p.rung[r];
-    lim.extend_to = std::min(lim.extend_to, lim.init_num);
-    lim.k = k;
-    EFG_TRY(search_device_ex(idx, L->bq.p + start[r] * ld, c, ld, lim, nullptr, nullptr, L->bout.p + start[r] * k, s,
-                             false, S ? L->bseeds.p + start[r] * S : nullptr, S));
-  }
-  permute_rows_kernel<true, int32_t><<<(unsigned)std::min<uint64_t>((nq * k + 255) / 256, 152 * 16), 256, 0, s>>>(
-      L->bout.p, L->perm.p, nq, k, d_out);
-  EFG_CUDA(cudaGetLastError());
-  return EFG_OK;
+  return search_device_ex(idx, d_q, nq, row_stride, lim, L->qp.p, nullptr, d_out, s, false,
+                          (E && m) ? L->seeds.p : nullptr, E * m);
 }
 
 int efg_learned_get_stats(const efg_learned* L, efg_learned_stats* out) {

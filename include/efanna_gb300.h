@@ -217,9 +217,7 @@ int efg_learned_train(efg_learned* lr, const float* d_queries, uint64_t n, uint6
 int efg_learned_predict_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
                                float coverage, uint32_t* d_clusters, uint32_t* d_rung, void* stream);
 /* Learned search: prediction, then the seeded nnexp search with each query at its predicted rung
- * shifted by rung_bias (clamped to the ladder); nq rows of k ids into d_out.  The queries are
- * grouped by rung (a stable order) and each group runs as one launch with that rung's parameters;
- * the call waits for the prediction to read the group sizes. */
+ * shifted by rung_bias (clamped to the ladder); nq rows of k ids into d_out. */
 int efg_learned_search_device(efg_learned* lr, const float* d_queries, uint64_t nq, uint64_t row_stride,
                               uint32_t k, float coverage, int rung_bias, int32_t* d_out, void* stream);
 int efg_learned_get_stats(const efg_learned* lr, efg_learned_stats* out);

@@ -507,7 +507,8 @@ def measure_batching(E, X, args):
            "batch_size": {"median": int(np.median(sizes)), "max": int(max(sizes))},
            "recall@k": round(recall_all, 4), "extend_scale_per_k": {str(k): v for k, v in chosen.items()},
            "ladder": ladder,
-           "plan_threads": plan.threads, "graph": "K=20 (trees 8, ml 8, iter 8, L 40, check 25, S 10)",
+           "plan_threads": plan.threads, "plan_config": plan.config,
+           "graph": "K=20 (trees 8, ml 8, iter 8, L 40, check 25, S 10)",
            "graph_build_s": round(build_s, 3), "in_flight": F,
            "one_in_flight": {"value": round(total / wall1, 1),
                              "batch_latency_ms": {"p50": round(float(np.percentile(lat1, 50)) * 1e3, 3),
@@ -515,7 +516,8 @@ def measure_batching(E, X, args):
            "ids_equal_to_one_in_flight": same,
            "form": "per-query k in {1,10,50,100}, pool = U(6,10) x extend; captured CUDA graphs replayed per "
                    "batch (host queries in, ids out) on %d plans with their own streams, scratch and pinned "
-                   "staging, %d batches in flight; persistent kernel, autotuned block size" % (F, F)}
+                   "staging, %d batches in flight; persistent kernel; autotuned block size, visited-set "
+                   "table size and CTAs per SM" % (F, F)}
     for pl in plans:
         pl.close()
     idx.close()

@@ -179,6 +179,7 @@ def lib():
         "efg_search_plan_collect": (i32, [vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_run": (i32, [vp, f32p, u64, u64, vp, C.POINTER(C.c_int32)]),
         "efg_search_plan_threads": (i32, [vp]),
+        "efg_search_plan_config": (i32, [vp, vp, vp, vp, vp, vp]),
         "efg_search_plan_destroy": (None, [vp]),
         "efg_learned_default_params": (None, [C.POINTER(LearnedParams)]),
         "efg_learned_create": (i32, [vp, C.POINTER(LearnedParams), C.POINTER(vp)]),
@@ -408,6 +409,16 @@ class SearchPlan:
     @property
     def threads(self) -> int:
         return lib().efg_search_plan_threads(self._h)
+
+    @property
+    def config(self) -> dict:
+        """The launch the autotuner chose: threads, ctas_per_sm (0: as many as fit), ht_pct (shared
+        visited-set size in percent of the default), variants timed, tuned_ms."""
+        v = [C.c_int32() for _ in range(4)]
+        ms = C.c_double()
+        _check(lib().efg_search_plan_config(self._h, *[C.byref(x) for x in v], C.byref(ms)))
+        return {"threads": v[0].value, "ctas_per_sm": v[1].value, "ht_pct": v[2].value, "variants": v[3].value,
+                "tuned_ms": round(ms.value, 3)}
 
     def run(self, queries: np.ndarray, params, out: np.ndarray | None = None) -> np.ndarray:
         q = np.ascontiguousarray(queries, dtype=np.float32)

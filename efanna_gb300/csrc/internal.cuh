@@ -147,6 +147,8 @@ struct efg_index {
   efg::DevBuf<uint32_t> kg_bits;
   efg::DevBuf<efg_query_params> qp_buf;  // per-query parameters of a host batch
   int search_threads = 0;                  // nnexp block size forced by a plan's autotuner (0: by occupancy)
+  int search_ctas_per_sm = 0;              // cap on resident nnexp CTAs per SM (0: as many as fit)
+  int search_ht_pct = 0;                   // shared visited-set size, percent of the default (0: 100)
   uint32_t candidate_cap = 0;              // bound on the nnexp candidate buffer (0: extend_to x degree)
 };
 

@@ -4,8 +4,10 @@
 // batches in flight side by side (submit / collect).  The batch size travels in
 // a device counter, so one graph serves every batch size up to the plan's capacity; the kernel is
 // persistent (a grid of resident CTAs looping over the batch's queries), and each query brings its
-// own pool size, extend, epochs and k.  An optional autotuner times the 256- and 512-thread builds
-// on calibration queries and keeps the faster one.
+// own pool size, extend, epochs and k.  An optional autotuner times launch variants on calibration
+// queries at the limits' parameters and keeps the fastest: the block size (256 or 512 threads), the
+// shared visited-set table (half, the default or double size; sets that outgrow it move to global
+// scratch) and the CTAs resident per SM (as many as fit, or one).  None of these changes a result.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -19,7 +21,11 @@ struct efg_search_plan {
   efg_index* idx = nullptr;
   uint64_t capacity = 0;
   efg_query_params lim{};
-  int threads = 0;
+  int threads = 0;       // the tuned launch: block size (0: by occupancy), CTAs per SM cap (0: none),
+  int ctas_per_sm = 0;   // shared visited-set size in percent of the default (0: 100)
+  int ht_pct = 0;
+  double tuned_ms = 0;   // the chosen variant's time on the calibration batch
+  int variants = 0;      // variants timed
   cudaStream_t stream = nullptr;  // the plan's own: plans of one index run side by side
   cudaEvent_t done = nullptr;     // the last submitted batch's ids are in hout
   DevBuf<float> q;
@@ -95,10 +101,18 @@ int stage_batch(efg_search_plan* p, const float* queries, uint64_t nq, uint64_t 
   return EFG_OK;
 }
 
-// Times one block-size build on the calibration batch already staged (median of three runs).
-int time_variant(efg_search_plan* p, int threads, uint64_t n_calib, double* ms) {
+// One launch variant of the nnexp search.
+struct Variant {
+  int threads, ht_pct, ctas_per_sm;
+};
+
+// Times one launch variant on the calibration batch already staged (median of three runs after a
+// warm-up).
+int time_variant(efg_search_plan* p, const Variant& v, uint64_t n_calib, double* ms) {
   efg_index* idx = p->idx;
-  idx->search_threads = threads;
+  idx->search_threads = v.threads;
+  idx->search_ht_pct = v.ht_pct;
+  idx->search_ctas_per_sm = v.ctas_per_sm;
   double best[3];
   for (int r = 0; r < 4; ++r) {
     auto t0 = std::chrono::steady_clock::now();
@@ -112,6 +126,19 @@ int time_variant(efg_search_plan* p, int threads, uint64_t n_calib, double* ms) 
   *ms = best[1];
   return EFG_OK;
 }
+
+// The index's launch knobs, kept aside while a plan tunes and captures its own.
+struct KnobGuard {
+  efg_index* idx;
+  int t, h, c;
+  explicit KnobGuard(efg_index* i)
+      : idx(i), t(i->search_threads), h(i->search_ht_pct), c(i->search_ctas_per_sm) {}
+  ~KnobGuard() {
+    idx->search_threads = t;
+    idx->search_ht_pct = h;
+    idx->search_ctas_per_sm = c;
+  }
+};
 
 int plan_build(efg_search_plan* p, const float* calib_queries, uint64_t n_calib) {
   efg_index* idx = p->idx;
@@ -134,17 +161,43 @@ int plan_build(efg_search_plan* p, const float* calib_queries, uint64_t n_calib)
   EFG_CUDA(cudaMemsetAsync(p->q.p, 0, capacity * idx->ld * sizeof(float), p->stream));
   EFG_CUDA(cudaStreamSynchronize(idx->stream));  // the index is built and idle
   ScratchSwap swap(p);
-  // autotune the block size on the calibration queries, all at the limits' parameters
+  KnobGuard knobs(idx);
+  // autotune the launch on the calibration queries, all at the limits' parameters
   if (calib_queries && n_calib) {
     uint64_t nc = std::min(n_calib, capacity);
     std::vector<efg_query_params> cp(nc, p->lim);
     EFG_TRY(stage_batch(p, calib_queries, nc, idx->dim, cp.data()));
-    double t256 = 0, t512 = 0;
-    EFG_TRY(time_variant(p, 256, nc, &t256));
-    EFG_TRY(time_variant(p, 512, nc, &t512));
-    p->threads = t512 < t256 ? 512 : 256;
+    const Variant variants[] = {{256, 100, 0}, {512, 100, 0}, {256, 50, 0},  {512, 50, 0}, {256, 200, 0},
+                                {512, 200, 0}, {256, 100, 1}, {256, 50, 1}, {256, 200, 1}};
+    double best = 1e300;
+    Variant pick = variants[0];
+    std::vector<int32_t> ref, got(nc * p->lim.k);
+    for (const Variant& v : variants) {
+      double ms = 0;
+      if (time_variant(p, v, nc, &ms) != EFG_OK) {  // a variant whose state does not fit: skipped
+        cudaGetLastError();
+        continue;
+      }
+      // every variant must return the same ids (the knobs change only where and how fast)
+      EFG_CUDA(cudaMemcpyAsync(got.data(), p->out.p, got.size() * 4, cudaMemcpyDeviceToHost, p->stream));
+      EFG_CUDA(cudaStreamSynchronize(p->stream));
+      if (ref.empty()) ref = got;
+      else if (ref != got) return fail(EFG_ERR_STATE, "launch variants returned different ids");
+      ++p->variants;
+      if (ms < best) {
+        best = ms;
+        pick = v;
+      }
+    }
+    if (!p->variants) return fail(EFG_ERR_ARG, "no launch variant fits the plan's parameter limits");
+    p->threads = pick.threads;
+    p->ht_pct = pick.ht_pct;
+    p->ctas_per_sm = pick.ctas_per_sm;
+    p->tuned_ms = best;
   }
   idx->search_threads = p->threads;
+  idx->search_ht_pct = p->ht_pct;
+  idx->search_ctas_per_sm = p->ctas_per_sm;
   // size every buffer and kernel attribute for the full capacity with an empty batch, then capture
   *p->hnq = 0;
   EFG_CUDA(cudaMemcpyAsync(p->nq.p, p->hnq, 4, cudaMemcpyHostToDevice, p->stream));
@@ -224,6 +277,17 @@ int efg_search_plan_run(efg_search_plan* p, const float* queries, uint64_t nq, u
 }
 
 int efg_search_plan_threads(const efg_search_plan* p) { return p ? p->threads : 0; }
+
+int efg_search_plan_config(const efg_search_plan* p, int32_t* threads, int32_t* ctas_per_sm, int32_t* ht_pct,
+                           int32_t* variants, double* tuned_ms) {
+  if (!p) return fail(EFG_ERR_ARG, "null plan");
+  if (threads) *threads = p->threads;
+  if (ctas_per_sm) *ctas_per_sm = p->ctas_per_sm;
+  if (ht_pct) *ht_pct = p->ht_pct;
+  if (variants) *variants = p->variants;
+  if (tuned_ms) *tuned_ms = p->tuned_ms;
+  return EFG_OK;
+}
 
 void efg_search_plan_destroy(efg_search_plan* p) {
   if (!p) return;

@@ -332,6 +332,8 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   };
   uint64_t big = nice(worst * 8 / 5 + 64);
   uint64_t small = std::min<uint64_t>(std::max<uint64_t>(nice(expect * 8 / 5), 2048), 12288);
+  if (idx->search_ht_pct > 0)  // a plan's autotuner scales the shared table (sets that outgrow it migrate)
+    small = std::max<uint64_t>(2048, nice(small * (uint64_t)idx->search_ht_pct / 100));
   small = std::min(small, big);
   if (big > (1ull << 28)) return fail(EFG_ERR_ARG, "search parameters visit too many candidates");
   // block size: 256 threads when several CTAs fit on an SM, else 512 threads
@@ -341,7 +343,7 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
     SearchCfg t = cfg;
     smem_probe = s256::layout(t, idx->ld, maxdeg, false, (uint32_t)small);
     EFG_CUDA(cudaFuncSetAttribute(s256::nnexp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::min<size_t>(smem_probe, 227 * 1024)));
+                                  (int)std::min<size_t>(smem_probe, 220 * 1024)));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, s256::nnexp_kernel, 256, smem_probe);
   }
   // block size: the autotuned choice when one is set, else 256 threads when two CTAs fit on an SM
@@ -369,6 +371,7 @@ int launch_nnexp(efg_index* idx, SearchCfg cfg, uint32_t maxdeg, const float* d_
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem1);
+  if (idx->search_ctas_per_sm > 0) per_sm = std::min(per_sm, idx->search_ctas_per_sm);
   uint64_t grid1 = std::min<uint64_t>(nq, (uint64_t)sms * std::max(1, per_sm));
   uint64_t grid2 = (uint64_t)sms;
   if (c1.ht_global) EFG_TRY(idx->ht_scratch.reserve(grid1 * c1.ht_size));

@@ -293,6 +293,13 @@ int efg_search_plan_run(efg_search_plan* plan, const float* queries, uint64_t nq
                         const efg_query_params* params, int32_t* out_ids);
 /* Block size the autotuner chose (256 or 512; 0 when the plan chose by occupancy). */
 int efg_search_plan_threads(const efg_search_plan* plan);
+/* The launch the plan's autotuner chose (all 0 when it was created without calibration queries):
+ * block size (256 or 512), cap on resident CTAs per SM (0: as many as fit), shared visited-set
+ * table in percent of the default size (sets that outgrow it move to global scratch; 0: 100), the
+ * number of variants timed and the chosen one's time on the calibration batch.  Any pointer may be
+ * NULL. */
+int efg_search_plan_config(const efg_search_plan* plan, int32_t* threads, int32_t* ctas_per_sm, int32_t* ht_pct,
+                           int32_t* variants, double* tuned_ms);
 void efg_search_plan_destroy(efg_search_plan* plan);
 
 /* File I/O, byte-compatible with the reference's formats. */

@@ -83,6 +83,12 @@ def test_search_plan_replays(efg, setup, calibrate):
     idx, q, _, oracle = setup
     plan = idx.search_plan(128, (6, 1000, 150, 100), calib=q[:64] if calibrate else None)
     assert plan.threads in ((256, 512) if calibrate else (0,))
+    cfg = plan.config
+    if calibrate:  # the autotuner's record (plan creation also checked that every variant gave the same ids)
+        assert cfg["variants"] >= 2 and cfg["tuned_ms"] > 0
+        assert cfg["ht_pct"] in (50, 100, 200) and cfg["ctas_per_sm"] in (0, 1)
+    else:
+        assert cfg == {"threads": 0, "ctas_per_sm": 0, "ht_pct": 0, "variants": 0, "tuned_ms": 0.0}
     rng = np.random.default_rng(2)
     for size in [1, 128, 37, 100]:
         rows = rng.choice(q.shape[0], size, replace=False)
@@ -166,3 +172,4 @@ def test_seeded_search_matches_oracle(efg, oracle_lib, setup):
                                  S.data_ptr(), 48, out.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), ref2)
+

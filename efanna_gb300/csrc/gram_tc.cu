@@ -44,6 +44,7 @@
 #include <mutex>
 
 #include "internal.cuh"
+#include "tcgen05.cuh"
 
 namespace efg {
 
@@ -64,11 +65,9 @@ template <int EW>
 constexpr uint32_t kThreads = 64 + 32 * EW;
 constexpr uint32_t MAX_STAGES = 8;
 constexpr uint32_t TMEM_COLS = 2 * TN;  // two FP32 accumulators of 128 columns
-constexpr unsigned long long WAIT_CYCLES = 4000000000ull;  // about 2 s at 2 GHz
 
-// instruction descriptor of tcgen05.mma.kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
-// (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17, M >> 4 at bit 24
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((TN >> 3) << 17) | ((TM >> 4) << 24);
+constexpr uint32_t IDESC = tc::idesc_bf16(TM, TN);
+using namespace tc;
 
 struct TcArgs {
   const float* qnorm;  // nq FP32 squared norms
@@ -81,94 +80,12 @@ struct TcArgs {
   uint32_t o_list, o_scr, o_xn;  // byte offsets of the lists, scratch and norm copies in dynamic shared memory
 };
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// Waits for the phase of `parity` to complete; false when the CTA is aborting or the wait ran out
-// (which also starts the abort).
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err) {
-  unsigned long long t0 = clock64();
-  for (uint32_t i = 0;; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 127) == 127) {
-      if (*abort_flag) return false;
-      if (clock64() - t0 > WAIT_CYCLES) {
-        *abort_flag = 1;
-        atomicOr(err, 1);
-        return false;
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor of a 128-row block of K-major BF16 rows, 128 bytes per row, in
-// the 128-byte swizzle layout TMA writes: 8-row groups 1024 bytes apart (stride byte offset),
-// descriptor version 1 (bits 46-47), swizzle mode 2 = 128 bytes (bits 61-63).  The block must
-// start on a 1024-byte boundary; the k-th 16-value slice starts 32 * k bytes further.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-// 32 lanes x 16 consecutive FP32 columns: thread i of the warp receives the 16 values of TMEM lane
-// (lane base + i) from the address's column on.  Asynchronous until tmem_wait().
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
 __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
   tmem_ld16(taddr, r);
   tmem_ld16(taddr + 16, r + 16);
   tmem_ld16(taddr + 32, r + 32);
   tmem_ld16(taddr + 48, r + 48);
 }
-__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Inserts a key into a thread's sorted list of at most K2 keys (a full list drops its last key).
 // Lists are slot-major with a stride of LS (the screening threads), so the threads of a warp touch
@@ -292,7 +209,7 @@ __global__ void __launch_bounds__(kThreads<EW>, 1)
 #pragma unroll
             for (uint32_t j = 0; j < TKB / 16; ++j) {  // K = 16 per MMA: 32 bytes further along the row
               const uint64_t o = (uint64_t)(2 * j);
-              umma_bf16(d_tmem, dq + o, dx + o, (step | j) != 0 ? 1u : 0u);
+              umma_bf16(d_tmem, dq + o, dx + o, IDESC, (step | j) != 0 ? 1u : 0u);
             }
             mma_issued = true;
             umma_commit(smem_addr(&bar_empty[s]));  // frees the stage when these MMAs have read it
@@ -524,39 +441,6 @@ __global__ void bound_kernel(const uint64_t* __restrict__ lists, uint64_t nq, ui
     if (prev) bnd = fminf(bnd, prev[qi]);
     out[qi] = bnd;
   }
-}
-
-// cuTensorMapEncodeTiled from the driver, found once through the runtime (no link against libcuda).
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_fn() {
-  static std::once_flag once;
-  static EncodeTiledFn fn = nullptr;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  });
-  return fn;
-}
-
-// Tensor map of `rows` BF16 rows of W values (W a multiple of 64): boxes of 64 values x 128 rows,
-// 128-byte swizzle; rows past the end read as zeros.
-int make_map(CUtensorMap* m, const __nv_bfloat16* p, uint64_t rows, uint32_t W) {
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return fail(EFG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  cuuint64_t dims[2] = {W, rows};
-  cuuint64_t strides[1] = {(cuuint64_t)W * 2};
-  cuuint32_t box[2] = {TKB, TM};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(p), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(EFG_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-  return EFG_OK;
 }
 
 }  // namespace

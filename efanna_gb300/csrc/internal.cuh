@@ -1,5 +1,6 @@
 // Internal declarations shared by the efanna_gb300 translation units.
 #pragma once
+#include <cuda_bf16.h>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -170,6 +171,10 @@ extern thread_local efg_knn_stats g_knn_stats;  // the calling thread's last ten
 int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
                        uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
                        cudaStream_t s, int force_split = 0);
+// mlp_tc.cu: the learned form's dense layers on the tensor cores, C = act(A W^T + bias) (A: M x K,
+// W: N x K, BF16 row-major; C FP32 and / or Cb BF16, M x N); EFG_ERR_ARG when the shape does not fit.
+int tc_gemm_bf16(uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat16* A, const __nv_bfloat16* W,
+                 const float* bias, int relu, float* C, __nv_bfloat16* Cb, int* err, cudaStream_t s);
 // The exact k-NN of the library: tensor-core screening where k allows, else the FP32 kernels.
 inline int exact_knn(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
                      uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,

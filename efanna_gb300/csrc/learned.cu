@@ -18,7 +18,9 @@
 //      loss = softmax cross-entropy of the cluster logits against the neighbour-cluster histogram
 //      plus softmax cross-entropy of the rung logits against the label, averaged over the batch.
 //      GEMM operands are BF16 (weights and activations; master weights FP32), accumulation FP32,
-//      gradients FP32, Adam on the master weights.
+//      gradients FP32, Adam on the master weights.  The forward layers run on the tensor cores
+//      (mlp_tc.cu: tcgen05 MMAs, bias and ReLU in the epilogue) where their inner size allows
+//      (64 <= K <= 256, K a multiple of 8); the rest, and the gradient GEMMs, on CUDA cores.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -446,6 +448,7 @@ struct efg_learned {
   DevBuf<float> h1, h2, z, dz, dh2, dh1;
   DevBuf<double> loss;
   DevBuf<uint32_t> pred_c, pred_r, seeds, batch_rows;
+  DevBuf<int> gerr;  // set by a tensor-core layer whose wait ran out (checked after training)
   DevBuf<efg_query_params> qp, ladder;
   efg_learned_stats stats{};
 };
@@ -470,22 +473,32 @@ int reserve_batch(efg_learned* L, uint64_t B) {
 }
 
 // Forward pass of B standardised rows already in L->xb: h1, h2 (FP32 and BF16) and logits z.
-void forward(efg_learned* L, uint32_t B, cudaStream_t s) {
+// One dense layer, act(A W^T + bias): on the tensor cores where the shape allows (64 <= K <= 256,
+// K a multiple of 8), else the CUDA-core GEMM.
+int dense(efg_learned* L, uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat16* A, const __nv_bfloat16* W,
+          const float* bias, int relu, float* C, __nv_bfloat16* Cb, cudaStream_t s) {
+  int rc = tc_gemm_bf16(M, N, K, A, W, bias, relu, C, Cb, L->gerr.p, s);
+  if (rc == EFG_OK) return EFG_OK;
+  if (rc != EFG_ERR_ARG) return rc;
+  gemm(M, N, K, A, K, 1, W, K, 1, bias, relu, (const float*)nullptr, C, Cb, s);
+  return EFG_OK;
+}
+
+int forward(efg_learned* L, uint32_t B, cudaStream_t s) {
   const uint32_t H = L->H, din = L->din, O = L->O;
   const __nv_bfloat16* W1 = L->wb.p + L->off[0];
   const __nv_bfloat16* W2 = L->wb.p + L->off[2];
   const __nv_bfloat16* W3 = L->wb.p + L->off[4];
-  gemm(B, H, din, L->xb.p, din, 1, W1, din, 1, L->w.p + L->off[1], 1, (const float*)nullptr, L->h1.p, L->h1b.p, s);
-  gemm(B, H, H, L->h1b.p, H, 1, W2, H, 1, L->w.p + L->off[3], 1, (const float*)nullptr, L->h2.p, L->h2b.p, s);
-  gemm(B, O, H, L->h2b.p, H, 1, W3, H, 1, L->w.p + L->off[5], 0, (const float*)nullptr, L->z.p,
-       (__nv_bfloat16*)nullptr, s);
+  EFG_TRY(dense(L, B, H, din, L->xb.p, W1, L->w.p + L->off[1], 1, L->h1.p, L->h1b.p, s));
+  EFG_TRY(dense(L, B, H, H, L->h1b.p, W2, L->w.p + L->off[3], 1, L->h2.p, L->h2b.p, s));
+  return dense(L, B, O, H, L->h2b.p, W3, L->w.p + L->off[5], 0, L->z.p, nullptr, s);
 }
 
 // Loss and gradients (into L->g) for B rows whose inputs are in L->xb and targets are trace rows
 // `rows` (or 0..B-1 when rows is null).
 int loss_and_grad(efg_learned* L, uint32_t B, const uint32_t* rows, cudaStream_t s, double* loss_out) {
   const uint32_t H = L->H, din = L->din, O = L->O;
-  forward(L, B, s);
+  EFG_TRY(forward(L, B, s));
   EFG_CUDA(cudaMemsetAsync(L->loss.p, 0, sizeof(double), s));
   softmax_ce_kernel<<<(B * 32 + 255) / 256, 256, 0, s>>>(L->z.p, B, O, L->Cn, L->R, L->tclusters.p, rows,
                                                         L->tlabel.p, L->dz.p, L->loss.p);
@@ -639,8 +652,10 @@ int efg_learned_create(efg_index* idx, const efg_learned_params* params, efg_lea
   std::vector<float> w;
   init_weights(L, w);
   if ((rc = L->w.reserve(np)) || (rc = L->g.reserve(np)) || (rc = L->m1.reserve(np)) || (rc = L->m2.reserve(np)) ||
-      (rc = L->wb.reserve(np)) || (rc = L->loss.reserve(1)) || (rc = L->ladder.reserve(L->R)))
+      (rc = L->wb.reserve(np)) || (rc = L->loss.reserve(1)) || (rc = L->ladder.reserve(L->R)) ||
+      (rc = L->gerr.reserve(1)))
     return bail(rc);
+  cudaMemsetAsync(L->gerr.p, 0, sizeof(int), s);
   cudaMemcpyAsync(L->w.p, w.data(), np * 4, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(L->m1.p, 0, np * 4, s);
   cudaMemsetAsync(L->m2.p, 0, np * 4, s);
@@ -746,7 +761,10 @@ int efg_learned_train(efg_learned* L, const float* d_q, uint64_t n, uint64_t row
     L->stats.train_loss_last = (float)mean_loss;
   }
   L->stats.train_queries = n;
+  int gerr = 0;
+  EFG_CUDA(cudaMemcpyAsync(&gerr, L->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   EFG_CUDA(cudaStreamSynchronize(s));
+  if (gerr) return fail(EFG_ERR_DEVICE_LIMIT, "a tensor-core layer's pipeline wait ran out");
   return EFG_OK;
 }
 
@@ -761,7 +779,7 @@ int efg_learned_predict_device(efg_learned* L, const float* d_q, uint64_t nq, ui
     uint32_t m = (uint32_t)std::min<uint64_t>(nq - q0, B);
     mlp_input_kernel<<<512, 256, 0, s>>>(d_q + q0 * row_stride, m, row_stride, L->din, nullptr, L->mean.p, L->istd.p,
                                          L->xb.p);
-    forward(L, m, s);
+    EFG_TRY(forward(L, m, s));
     predict_kernel<<<(m * 32 + 255) / 256, 256, 0, s>>>(L->z.p, m, L->O, L->Cn, L->R, L->p.entry_clusters,
                                                         coverage, d_clusters ? d_clusters + q0 * L->p.entry_clusters : nullptr,
                                                         d_rung + q0);

@@ -187,3 +187,36 @@ def test_learned_search_gains_over_plain_on_anisotropic_mixture(efg):
     assert gains and min(gains) <= 0.9, gains
     L.close()
     idx.close()
+
+
+def test_tensor_core_layers_match_cpu_oracle(efg):
+    """With d = 96 and 128 hidden units every forward layer runs on the tensor cores (tcgen05, inner
+    sizes 96 and 128): the loss and gradients still match the CPU oracle within the same bounds as
+    the CUDA-core layers."""
+    d, H = 96, 128
+    X = datasets.mixture_aniso_device(4000, d, seed=11)
+    x = X.cpu().numpy()
+    idx = efg.Index(x, efg.IndexParams(trees=4, merge_level=4, epochs=4, K=10))
+    idx.build_index()
+    idx.build_trees(4)
+    L = efg.Learned(idx, clusters=16, entries_per_cluster=4, entry_clusters=2, hidden=H, rungs=RUNGS,
+                    kmeans_iters=4, kmeans_sample=4000)
+    rng = np.random.default_rng(8)
+    B = 200
+    q = datasets.mixture_aniso_device(B, d, seed=11, queries=True).cpu().numpy()
+    tc = rng.integers(0, 16, (B, M.GT_K)).astype(np.uint32)
+    tl = rng.integers(0, len(RUNGS), B).astype(np.uint8)
+    w = L.weights() + rng.normal(0, 0.05, L.num_params()).astype(np.float32)
+    L.set_weights(w)
+    mean, istd = L.norm()
+    Q = torch.from_numpy(q).cuda()
+    TC = torch.from_numpy(tc.view(np.int32)).cuda()
+    TL = torch.from_numpy(tl).cuda()
+    loss, g = L.grad_device(Q.data_ptr(), B, d, TC.data_ptr(), TL.data_ptr())
+    rl, rg = M.loss_and_grad(w, q, mean, istd, tc.astype(np.int64), tl, 16, len(RUNGS), H)
+    assert abs(loss - rl) / abs(rl) < 1e-4
+    assert np.linalg.norm(g - rg) / np.linalg.norm(rg) < 2e-3
+    for part_g, part_r in zip(M.split(g, d, H, 16 + len(RUNGS)), M.split(rg, d, H, 16 + len(RUNGS))):
+        assert np.linalg.norm(part_g - part_r) <= 5e-3 * np.linalg.norm(part_r) + 1e-7
+    L.close()
+    idx.close()

@@ -472,7 +472,6 @@ int reserve_batch(efg_learned* L, uint64_t B) {
   return EFG_OK;
 }
 
-// Forward pass of B standardised rows already in L->xb: h1, h2 (FP32 and BF16) and logits z.
 // One dense layer, act(A W^T + bias): on the tensor cores where the shape allows (64 <= K <= 256,
 // K a multiple of 8), else the CUDA-core GEMM.
 int dense(efg_learned* L, uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat16* A, const __nv_bfloat16* W,
@@ -484,6 +483,7 @@ int dense(efg_learned* L, uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat1
   return EFG_OK;
 }
 
+// Forward pass of B standardised rows already in L->xb: h1, h2 (FP32 and BF16) and logits z.
 int forward(efg_learned* L, uint32_t B, cudaStream_t s) {
   const uint32_t H = L->H, din = L->din, O = L->O;
   const __nv_bfloat16* W1 = L->wb.p + L->off[0];
@@ -773,7 +773,7 @@ int efg_learned_predict_device(efg_learned* L, const float* d_q, uint64_t nq, ui
   if (!L || ((!d_q || !d_rung || (!d_clusters && L->p.entry_clusters)) && nq)) return fail(EFG_ERR_ARG, "null argument");
   if (row_stride < L->idx->dim) return fail(EFG_ERR_ARG, "row_stride < dim");
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t B = 4096;
+  const uint32_t B = 32768;  // queries per pass through the network
   EFG_TRY(reserve_batch(L, B));
   for (uint64_t q0 = 0; q0 < nq; q0 += B) {
     uint32_t m = (uint32_t)std::min<uint64_t>(nq - q0, B);

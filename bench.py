@@ -815,7 +815,7 @@ def measure_learned_aniso(E, args, n=None, decay=0.35, plain_ladder=None, rungs=
     rung = torch.zeros(nq, dtype=torch.int32, device="cuda")
     cl = torch.zeros((nq, 8), dtype=torch.int32, device="cuda")
     learned = []
-    for cov in (0.5, 0.6, 0.7, 0.8, 0.85, 0.9, 0.95, 0.98):
+    for cov in (0.5, 0.6, 0.7, 0.72, 0.74, 0.76, 0.78, 0.8, 0.82, 0.84, 0.86, 0.88, 0.9, 0.95, 0.98):
         f = lambda: L.search_device(Q.data_ptr(), nq, d, 10, out.data_ptr(), 0, stream.cuda_stream, cov)
         f()
         rc = rec_of()

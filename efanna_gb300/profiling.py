@@ -14,6 +14,10 @@
         builds the graph of one configuration from host data (the base drawn on the GPU for the
         unit and aniso generators and copied back) and reports the build's phases and the graph
         recall@K of 2000 sampled rows against their exact neighbours.
+    python -m efanna_gb300.profiling mlp [--n N] [--queries Q]
+        the learned form's prediction on the tensor cores: a 96-d anisotropic index of N points,
+        an untrained network (96-256-256-(1024 + 8)), Q queries predicted three times, and the
+        prediction rate.
     python -m efanna_gb300.profiling knn [--n N] [--nq Q] [--dim D] [--k K] [--data u8|unit]
                                          [--screening auto|fp32|split] [--repeat R]
         times the exact k-NN (tensor-core or FP32 screening) on seeded data: per call the
@@ -156,6 +160,34 @@ def build_case(n: int, dim: int, data: str, K: int, L: int, check: int, S: int, 
     idx.close()
 
 
+def mlp_case(n: int, nq: int) -> None:
+    import time
+
+    import torch
+
+    import efanna_gb300 as E
+    from efanna_gb300 import datasets
+    X = datasets.mixture_aniso_device(n, 96, seed=0)
+    Q = datasets.mixture_aniso_device(nq, 96, seed=0, queries=True)
+    idx = E.Index.from_device(X.data_ptr(), n, 96, 96, E.IndexParams(trees=4, merge_level=4, epochs=2, K=10))
+    idx.build_index()
+    idx.build_trees(4)
+    L = E.Learned(idx, clusters=1024, entries_per_cluster=8, entry_clusters=8, hidden=256,
+                  rungs=[(4, 200, 20), (4, 400, 40), (4, 600, 60), (4, 800, 80), (4, 1000, 100), (4, 1500, 150),
+                         (4, 2000, 200), (4, 3000, 300)], kmeans_iters=2, kmeans_sample=20000)
+    rung = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    cl = torch.zeros((nq, 8), dtype=torch.int32, device="cuda")
+    for r in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L.predict_device(Q.data_ptr(), nq, 96, cl.data_ptr(), rung.data_ptr(), 0, 0.9)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        print("mlp predict %d queries: %.3f ms, %.1f M queries/s" % (nq, dt * 1e3, nq / dt / 1e6), flush=True)
+    L.close()
+    idx.close()
+
+
 def search_case(n: int, nq: int, point, trees: int, extra=None, precisions=("fp32",), repeat: int = 2,
                 method: int = 0, recall: bool = False) -> None:
     import time
@@ -263,6 +295,9 @@ if __name__ == "__main__":
     b.add_argument("--trees", type=int, default=8)
     b.add_argument("--ml", type=int, default=8)
     b.add_argument("--iter", type=int, default=8)
+    ml = sub.add_parser("mlp")
+    ml.add_argument("--n", type=int, default=200000)
+    ml.add_argument("--queries", type=int, default=100000)
     kn = sub.add_parser("knn")
     kn.add_argument("--n", type=int, default=1000000)
     kn.add_argument("--nq", type=int, default=10000)
@@ -272,7 +307,9 @@ if __name__ == "__main__":
     kn.add_argument("--screening", default="auto", choices=["auto", "fp32", "split"])
     kn.add_argument("--repeat", type=int, default=3)
     a = ap.parse_args()
-    if a.cmd == "build":
+    if a.cmd == "mlp":
+        mlp_case(a.n, a.queries)
+    elif a.cmd == "build":
         build_case(a.n, a.dim, a.data, a.K, a.L, a.check, a.S, a.trees, a.ml, a.iter)
     elif a.cmd == "knn":
         knn_case(a.n, a.nq, a.dim, a.k, a.data, a.screening, a.repeat)

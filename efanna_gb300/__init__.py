@@ -42,7 +42,8 @@ class BuildParams(C.Structure):
 class BuildStats(C.Structure):
     _fields_ = [("trees_ms", C.c_double), ("init_ms", C.c_double), ("refine_ms", C.c_double),
                 ("total_ms", C.c_double), ("join_pairs", C.c_uint64), ("join_records", C.c_uint64),
-                ("merge_distances", C.c_uint64), ("max_merge_depth", C.c_int32)]
+                ("merge_distances", C.c_uint64), ("max_merge_depth", C.c_int32),
+                ("join_fp32_nodes", C.c_uint64)]
 
 
 class SearchStats(C.Structure):
@@ -150,6 +151,7 @@ def lib():
         "efg_get_build_stats": (i32, [vp, C.POINTER(BuildStats)]),
         "efg_set_search_params": (i32, [vp, i32, i32, i32, i32, i32, i32]),
         "efg_set_search_precision": (i32, [vp, i32]),
+        "efg_set_build_precision": (i32, [vp, i32]),
         "efg_set_search_candidate_cap": (i32, [vp, u32]),
         "efg_screen_distances": (i32, [vp, i32, vp, u64, u64, vp, u32, vp, vp]),
         "efg_knn_search": (i32, [vp, f32p, u64, u32, u64, u32, C.POINTER(C.c_int32)]),
@@ -293,6 +295,15 @@ class Index:
         if code is None:
             raise ValueError("precision must be 'fp32', 'bf16' or 'fp8'")
         _check(lib().efg_set_search_precision(self._h, code))
+
+    def set_build_precision(self, precision: str) -> None:
+        """'fp32' (the reference's join arithmetic, the default) or 'bf16': the NN-descent join's pair
+        distances as one Gram tile per node on the tensor cores (identical graph on byte data up to
+        128 dimensions; hi + lo BF16 products for other data)."""
+        code = {"fp32": 0, "bf16": 1}.get(precision)
+        if code is None:
+            raise ValueError("build precision must be 'fp32' or 'bf16'")
+        _check(lib().efg_set_build_precision(self._h, code))
 
     def set_search_candidate_cap(self, cap: int) -> None:
         """Bound on the nnexp search's per-query candidate buffer (0: the worst case, the default)."""

@@ -22,7 +22,7 @@ PHASE_OUT_DIR = os.path.join(HERE, "_build_phase")
 PHASE_LIB = os.path.join(HERE, "libefanna_gb300_phase.so")
 CLI_SRC = os.path.join(HERE, "cli", "efg_cli.cc")
 CLI = os.path.join(HERE, "cli", "efg_cli")
-SOURCES = ["index.cu", "distance.cu", "search.cu", "kgraph.cu", "plan.cu", "learned.cu", "hashing.cu", "trees.cu", "nndescent.cu", "noalloc.cu", "gram_tc.cu", "mlp_tc.cu"]
+SOURCES = ["index.cu", "distance.cu", "search.cu", "kgraph.cu", "plan.cu", "learned.cu", "hashing.cu", "trees.cu", "nndescent.cu", "noalloc.cu", "gram_tc.cu", "mlp_tc.cu", "join_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -393,6 +393,14 @@ int efg_set_search_precision(efg_index* idx, int precision) {
   return EFG_OK;
 }
 
+int efg_set_build_precision(efg_index* idx, int precision) {
+  if (!idx) return fail(EFG_ERR_ARG, "null index");
+  if (precision != EFG_PRECISION_FP32 && precision != EFG_PRECISION_BF16)
+    return fail(EFG_ERR_ARG, "build precision must be EFG_PRECISION_FP32 or EFG_PRECISION_BF16");
+  idx->build_precision = precision;
+  return EFG_OK;
+}
+
 int efg_screen_distances(efg_index* idx, int precision, const float* d_q, uint64_t nq, uint64_t row_stride,
                          const uint32_t* d_ids, uint32_t m, float* d_out, void* stream) {
   if (!idx || ((!d_q || !d_ids || !d_out) && nq && m)) return fail(EFG_ERR_ARG, "null argument");

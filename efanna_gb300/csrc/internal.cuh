@@ -138,6 +138,7 @@ struct efg_index {
   efg::DevBuf<uint32_t> ovf_list;    // queries handed from the first search pass to the overflow pass
   // search precision: 0 = FP32 rows, 1 = BF16 screening copy (base16, ld16 values per row) + FP32 re-rank
   int precision = 0;
+  int build_precision = 0;  // NN-descent join: EFG_PRECISION_FP32 or EFG_PRECISION_BF16 (tensor cores)
   efg::DevBuf<uint16_t> base16;
   uint32_t ld16 = 0;
   efg::DevBuf<uint8_t> base8;   // FP8 e4m3 screening copy (ld8 bytes per row) and per-row scales
@@ -171,6 +172,17 @@ extern thread_local efg_knn_stats g_knn_stats;  // the calling thread's last ten
 int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld, const float* q, uint64_t nq,
                        uint32_t qld, uint32_t k, int exclude_self, uint64_t first_row, int32_t* ids, float* dists,
                        cudaStream_t s, int force_split = 0);
+// join_tc.cu: the NN-descent join's pass 0 on the tensor cores.  tc_join_prepare converts the base
+// to BF16 hi / lo rows of round_up(dim, 64) values with FP32 norms and sets *inexact when some lo is
+// not zero; tc_join scores every node that fits one tile (<= 128 new, <= 256 rows) and lists the
+// others in big (big[0] their count) for join_dist_kernel; err is set when a wait ran out.
+int tc_join_prepare(const float* base, uint64_t n, uint32_t dim, uint32_t ld, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                    float* norms, int* inexact, cudaStream_t s);
+int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms, uint64_t n, uint32_t dim,
+            uint32_t terms, uint32_t cap, uint32_t P, uint32_t check_k, const uint32_t* new_ids,
+            const uint32_t* new_cnt, const uint32_t* old_ids, const uint32_t* old_cnt, const uint64_t* pair_off,
+            const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* next_node, uint32_t* big,
+            int* err, cudaStream_t s);
 // mlp_tc.cu: the learned form's dense layers on the tensor cores, C = act(A W^T + bias) (A: M x K,
 // W: N x K, BF16 row-major; C FP32 and / or Cb BF16, M x N); EFG_ERR_ARG when the shape does not fit.
 int tc_gemm_bf16(uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat16* A, const __nv_bfloat16* W,

@@ -27,6 +27,7 @@
 #include <cfloat>
 #include <vector>
 
+#include "join.cuh"
 #include "scan.cuh"
 #include "warpsort.cuh"
 
@@ -46,12 +47,20 @@ struct NNDev {
   DevBuf<float> pairdist;
   DevBuf<uint32_t> cnt, cursor, rec_aux, rcnt, rcur, roff, rbuf, scan32, ucnt;
   DevBuf<uint64_t> rec_key;
+  // tensor-core join: BF16 rows (hi, lo), FP32 norms, flags {inexact, error}, nodes left to FP32
+  DevBuf<__nv_bfloat16> jhi, jlo;
+  DevBuf<float> jnorm;
+  DevBuf<int> jflag;
+  DevBuf<uint32_t> jbig;
+  uint32_t jterms = 0;  // 0: not prepared; 1 or 3 products per value
   void release_all() {
     pd.release(); radius.release(); radiusM.release(); pid.release(); Lc.release(); Range.release();
     new_ids.release(); new_cnt.release(); old_ids.release(); old_cnt.release(); found.release();
     pair_off.release(); rec_off64.release(); scan64.release(); pairdist.release(); cnt.release(); cursor.release();
     rec_aux.release(); rcnt.release(); rcur.release(); roff.release(); rbuf.release(); scan32.release();
-    ucnt.release(); rec_key.release();
+    ucnt.release(); rec_key.release(); jhi.release(); jlo.release(); jnorm.release(); jflag.release();
+    jbig.release();
+    jterms = 0;
   }
 };
 
@@ -411,73 +420,26 @@ __global__ void bound_kernel(uint64_t n, uint32_t P, const float* __restrict__ p
   bound[t] = r > w ? r : w;
 }
 
-// The record side of one join pair (a lane's pair): x is the list entry being joined, y the
-// candidate, my_new whether y comes from the new list, slot its pairdist index.  Pass 0 stores the
-// distance and counts the records per target; pass 1 reads it back and writes the records.
-// Returns whether side 0 dropped a candidate that a rank below check_k could have needed.
-template <int PASS>
-__device__ __forceinline__ bool join_lane_record(uint64_t i, uint32_t x, uint32_t y, bool my_new, float mine,
-                                                 uint64_t slot, uint32_t P, uint32_t check_k,
-                                                 const float* __restrict__ bound, float* __restrict__ pairdist,
-                                                 uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off,
-                                                 uint32_t* __restrict__ cursor, uint64_t* __restrict__ rec_key,
-                                                 uint32_t* __restrict__ rec_aux) {
-  const bool same = my_new && y == x;  // equal ids: no pair
-  if (PASS == 0) pairdist[slot] = same ? __int_as_float(0x7fc00000) : mine;
-  else mine = pairdist[slot];
-  if (same) return false;
-  uint32_t a = x, b = y;
-  if (my_new && b < a) {
-    a = y;
-    b = x;
-  }
-  bool drop = false;
-  // side 0: candidate b into node a (its rank feeds found); side 1: a into b
-  if (mine <= bound[a]) {
-    if (PASS == 0) atomicAdd(&cnt[a], 1u);
-    else {
-      uint32_t pos = atomicAdd(&cursor[a], 1u);
-      rec_key[rec_off[a] + pos] = pack_key(mine, b);
-      rec_aux[rec_off[a] + pos] = (uint32_t)(i << 1);
-    }
-  } else if (P < check_k) {
-    drop = true;
-  }
-  if (mine <= bound[b]) {
-    if (PASS == 0) atomicAdd(&cnt[b], 1u);
-    else {
-      uint32_t pos = atomicAdd(&cursor[b], 1u);
-      rec_key[rec_off[b] + pos] = pack_key(mine, a);
-      rec_aux[rec_off[b] + pos] = (uint32_t)(i << 1) | 1u;
-    }
-  }
-  return drop;
-}
-
-// pairdist index of node i's pair (new entry p, candidate c): the pairs of p' < p come first.
-__device__ __forceinline__ uint64_t join_slot(uint64_t po, uint32_t nn, uint32_t no, uint32_t p, uint32_t c) {
-  uint64_t sp = p == 0 ? 0 : (uint64_t)p * (nn - 1) - (uint64_t)p * (p - 1) / 2 + (uint64_t)p * no;
-  return po + sp + c;
-}
-
 // Join pass 0: the distances of node i's pairs, stored, and record counts per target.  One warp
 // per node, nodes taken from a shared counter as warps come free (pair counts differ by an order
 // of magnitude, so a fixed assignment leaves most warps of a block idle behind its longest node).
 // New entries are taken two at a time: x0 = new[p] pairs with Y = new[p+1..] + old, x1 = new[p+1]
 // with Y[1..], so every candidate row loaded serves both; four rows per pass, the 2 x 4 sums
-// reduced together.
+// reduced together.  With a node list (list[0] nodes, their ids from list[1]) only those nodes.
 __global__ void __launch_bounds__(256, 4) join_dist_kernel(
     const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P, uint32_t check_k,
     const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids,
     const uint32_t* __restrict__ old_cnt, const uint64_t* __restrict__ pair_off, const float* __restrict__ bound,
     float* __restrict__ pairdist, uint32_t* __restrict__ cnt, uint8_t* __restrict__ found,
-    uint32_t* __restrict__ next_node) {
+    uint32_t* __restrict__ next_node, const uint32_t* __restrict__ list) {
   const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nodes = list ? list[0] : n;
   for (;;) {
     uint32_t ii = 0;
     if (lane == 0) ii = atomicAdd(next_node, 1u);
-    const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
-    if (i >= n) return;
+    ii = __shfl_sync(0xffffffffu, ii, 0);
+    if (ii >= nodes) return;
+    const uint64_t i = list ? list[1 + ii] : ii;
     const uint32_t nn = new_cnt[i], no = old_cnt[i];
     if (nn == 0) continue;
     const uint32_t* nw = new_ids + i * cap;
@@ -609,9 +571,13 @@ __device__ __forceinline__ K96 next_batch(const uint64_t* __restrict__ rk, const
 }
 
 // One warp per target node: applies its records in ascending (dist, id, source, side) order
-// with Neighbor::insert / InsertIntoKnn semantics.
+// with Neighbor::insert / InsertIntoKnn semantics (base_index.hpp:37-61).  The reference rejects
+// a candidate whose id sits among the entries of equal distance; a pair's distance is the same
+// wherever the reference computes it, so that finds every repeat.  With any_dist a repeat is found
+// at any distance: the tensor-core join's distances can differ in the last bits from the FP32
+// ones a pool entry was inserted with, and an equal-distance test would let the id in twice.
 template <int NS>
-__global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, const uint32_t* __restrict__ cnt,
+__global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_dist, const uint32_t* __restrict__ cnt,
                              const uint64_t* __restrict__ rec_off, const uint64_t* __restrict__ rec_key,
                              const uint32_t* __restrict__ rec_aux, float* __restrict__ pd,
                              uint32_t* __restrict__ pid, uint32_t* __restrict__ Lc, float* __restrict__ radius,
@@ -670,7 +636,8 @@ __global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, const uin
 #pragma unroll
       for (int s = 0; s < NS; ++s) {
         uint32_t e = s * 32 + lane;
-        dup |= __ballot_sync(0xffffffffu, e < i && pool.d[s] == d && (pool.id[s] & IDM) == cand);
+        dup |= __ballot_sync(0xffffffffu, (any_dist ? e < L : (e < i && pool.d[s] == d)) &&
+                                              (pool.id[s] & IDM) == cand);
       }
       if (dup) {
         rank = L + 1;
@@ -849,12 +816,16 @@ __global__ void update_reverse_kernel(uint64_t n, uint32_t cap, uint32_t rcap, u
       run = warp_merge_min32(run, x);
     }
     first = false;
+    // a source listed twice (a pool holding an id twice) leaves fewer distinct keys than take:
+    // the list ends at the last one
     uint32_t got = min(32u, take - done);
+    got = min(got, (uint32_t)__popc(__ballot_sync(0xffffffffu, run != ~0ULL)));
     if (lane < got) ids[c0 + done + lane] = (uint32_t)run;
+    if (got == 0) break;
     last = __shfl_sync(0xffffffffu, run, got - 1);
     done += got;
   }
-  if (lane == 0) *cntp = c0 + take;
+  if (lane == 0) *cntp = c0 + done;
 }
 
 __global__ void export_graph_kernel(uint64_t n, uint32_t P, uint32_t K, const uint32_t* __restrict__ pid,
@@ -1016,9 +987,9 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.found.p, 0, n, s));
-  LocalBuf<uint32_t> jctr;  // node counters of the two join passes and the merge
-  EFG_TRY(jctr.reserve(3));
-  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 12, s));
+  LocalBuf<uint32_t> jctr;  // node counters of the two join passes, the merge and the FP32 node list
+  EFG_TRY(jctr.reserve(4));
+  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 16, s));
   int sms = 152, per0 = 1, per1 = 1, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1026,15 +997,45 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, join_records_kernel, 256, 0);
   const unsigned jgrid0 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per0, 1));
   const unsigned jgrid1 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per1, 1));
+  const bool tc = idx->build_precision == EFG_PRECISION_BF16;
+  if (tc) {
+    // pass 0 on the tensor cores; nodes too large for one tile go to the FP32 kernel's node list
+    if (!S.jterms) {
+      const uint64_t W = (idx->dim + 63) / 64 * 64;
+      EFG_TRY(S.jhi.reserve(n * W));
+      EFG_TRY(S.jlo.reserve(n * W));
+      EFG_TRY(S.jnorm.reserve(n));
+      EFG_TRY(S.jflag.reserve(2));
+      EFG_TRY(S.jbig.reserve(n + 1));
+      EFG_TRY(tc_join_prepare(idx->d_base, n, idx->dim, idx->ld, S.jhi.p, S.jlo.p, S.jnorm.p, S.jflag.p, s));
+      int inexact = 0;
+      EFG_CUDA(cudaMemcpyAsync(&inexact, S.jflag.p, 4, cudaMemcpyDeviceToHost, s));
+      EFG_CUDA(cudaStreamSynchronize(s));
+      S.jterms = inexact ? 3 : 1;
+    }
+    EFG_CUDA(cudaMemsetAsync(S.jflag.p + 1, 0, 4, s));
+    EFG_CUDA(cudaMemsetAsync(S.jbig.p, 0, 4, s));
+    EFG_TRY(tc_join(S.jhi.p, S.jlo.p, S.jnorm.p, n, idx->dim, S.jterms, S.cap, S.P, bp.check_k, S.new_ids.p,
+                    S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p, S.found.p,
+                    jctr.p, S.jbig.p, S.jflag.p + 1, s));
+  }
   join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
                                           S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
-                                          S.found.p, jctr.p);
+                                          S.found.p, tc ? jctr.p + 3 : jctr.p, tc ? S.jbig.p : nullptr);
   EFG_CUDA(cudaGetLastError());
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, tmp64.p, n);
   EFG_TRY(device_scan<uint64_t>(tmp64.p, n, S.rec_off64.p, S.scan64.p, s));
   uint64_t nrec = 0;
   EFG_CUDA(cudaMemcpyAsync(&nrec, S.rec_off64.p + n, 8, cudaMemcpyDeviceToHost, s));
+  int jstat[2] = {0, 0};  // tensor-core join: error word, nodes left to the FP32 kernel
+  if (tc) {
+    EFG_CUDA(cudaMemcpyAsync(&jstat[0], S.jflag.p + 1, 4, cudaMemcpyDeviceToHost, s));
+    EFG_CUDA(cudaMemcpyAsync(&jstat[1], S.jbig.p, 4, cudaMemcpyDeviceToHost, s));
+  }
   EFG_CUDA(cudaStreamSynchronize(s));
+  if (jstat[0] & 4) return fail(EFG_ERR_ARG, "tensor-core join: a join list holds an id >= n");
+  if (jstat[0]) return fail(EFG_ERR_DEVICE_LIMIT, "tensor-core join: a wait ran out on the device");
+  idx->bstats.join_fp32_nodes += (uint32_t)jstat[1];
   EFG_TRY(S.rec_key.reserve(nrec + 1));
   EFG_TRY(S.rec_aux.reserve(nrec + 1));
   join_records_kernel<<<jgrid1, 256, 0, s>>>(n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p,
@@ -1043,16 +1044,16 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaGetLastError());
   const unsigned mgrid = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * 8);
   if (S.P <= 32)
-    merge_kernel<1><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+    merge_kernel<1><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
                                           S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else if (S.P <= 64)
-    merge_kernel<2><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+    merge_kernel<2><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
                                           S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else if (S.P <= 128)
-    merge_kernel<4><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+    merge_kernel<4><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
                                           S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   else
-    merge_kernel<8><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
+    merge_kernel<8><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
                                           S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
   EFG_CUDA(cudaGetLastError());
   // ---- update

@@ -111,6 +111,35 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
 // Waits for every tcgen05.ld this thread issued.
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// FP32 rows -> BF16 hi (and lo = x - hi) rows of W values (zero padded), FP32 squared norms (+inf
+// for the padding rows up to norm_rows), and a flag set when some lo is not zero.  A warp per row.
+static __global__ void to_bf16_kernel(const float* __restrict__ src, uint64_t rows, uint32_t dim, uint64_t ld, uint32_t W,
+                               __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                               float* __restrict__ norms, uint64_t norm_rows, int* __restrict__ inexact) {
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < norm_rows; r += nw) {
+    if (r >= rows) {
+      if (lane == 0) norms[r] = INFINITY;
+      continue;
+    }
+    float acc = 0.f;
+    bool any_lo = false;
+    for (uint32_t c = lane; c < W; c += 32) {
+      const float x = c < dim ? src[r * ld + c] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+      hi[r * W + c] = h;
+      lo[r * W + c] = l;
+      any_lo |= __bfloat162float(l) != 0.f;
+      acc = fmaf(x, x, acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) norms[r] = acc;
+    if (__any_sync(0xffffffffu, any_lo) && lane == 0) atomicOr(inexact, 1);
+  }
+}
+
 // cuTensorMapEncodeTiled from the driver, found once through the runtime (no link against libcuda).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,

@@ -127,7 +127,7 @@ def make_base(n: int, dim: int, data: str, seed: int = 0, queries: bool = False)
 
 
 def build_case(n: int, dim: int, data: str, K: int, L: int, check: int, S: int, trees: int, ml: int,
-               iters: int) -> None:
+               iters: int, precisions=("fp32",)) -> None:
     import time
 
     import torch
@@ -136,28 +136,32 @@ def build_case(n: int, dim: int, data: str, K: int, L: int, check: int, S: int, 
     t0 = time.perf_counter()
     x = make_base(n, dim, data)
     gen_s = time.perf_counter() - t0
-    idx = E.Index(x, E.IndexParams(trees=trees, merge_level=ml, epochs=iters, check=check, L=L, K=K, S=S))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    idx.build_index()
-    torch.cuda.synchronize()
-    build_s = time.perf_counter() - t0
-    st = idx.build_stats()
-    g = idx.graph()
-    rows = np.sort(np.random.default_rng(3).choice(n, min(n, 2000), replace=False))
     X = torch.from_numpy(x).cuda()
+    rows = np.sort(np.random.default_rng(3).choice(n, min(n, 2000), replace=False))
     S_ = X[torch.from_numpy(rows).cuda()].contiguous()
     gt = torch.zeros((len(rows), K + 1), dtype=torch.int32, device="cuda")
     E.brute_force_knn_device(X.data_ptr(), n, dim, dim, S_.data_ptr(), len(rows), dim, K + 1, gt.data_ptr())
     torch.cuda.synchronize()
     gtn = gt.cpu().numpy()
-    # the sampled rows are base rows: each one's exact K neighbours other than itself
-    rec = np.mean([len(set(g[r].tolist()) & set([v for v in gtn[i] if v != r][:K])) / K for i, r in enumerate(rows)])
-    print("build %s %d x %d K=%d L=%d check=%d S=%d trees=%d ml=%d iter=%d: data %.1f s, build %.3f s (trees %.1f ms, "
-          "init %.1f ms, refine %.1f ms), join pairs %d, records %d; graph recall@%d (2000 rows) %.4f"
-          % (data, n, dim, K, L, check, S, trees, ml, iters, gen_s, build_s, st.trees_ms, st.init_ms, st.refine_ms,
-             st.join_pairs, st.join_records, K, rec), flush=True)
-    idx.close()
+    for prec in precisions:
+        idx = E.Index(x, E.IndexParams(trees=trees, merge_level=ml, epochs=iters, check=check, L=L, K=K, S=S))
+        idx.set_build_precision(prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        idx.build_index()
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        st = idx.build_stats()
+        g = idx.graph()
+        # the sampled rows are base rows: each one's exact K neighbours other than itself
+        rec = np.mean([len(set(g[r].tolist()) & set([v for v in gtn[i] if v != r][:K])) / K
+                       for i, r in enumerate(rows)])
+        print("build %s %d x %d K=%d L=%d check=%d S=%d trees=%d ml=%d iter=%d join %s: data %.1f s, build %.3f s "
+              "(trees %.1f ms, init %.1f ms, refine %.1f ms), join pairs %d, records %d, FP32-kernel nodes %d; "
+              "graph recall@%d (2000 rows) %.4f"
+              % (data, n, dim, K, L, check, S, trees, ml, iters, prec, gen_s, build_s, st.trees_ms, st.init_ms,
+                 st.refine_ms, st.join_pairs, st.join_records, st.join_fp32_nodes, K, rec), flush=True)
+        idx.close()
 
 
 def mlp_case(n: int, nq: int) -> None:
@@ -295,6 +299,8 @@ if __name__ == "__main__":
     b.add_argument("--trees", type=int, default=8)
     b.add_argument("--ml", type=int, default=8)
     b.add_argument("--iter", type=int, default=8)
+    b.add_argument("--precision", nargs="+", default=["fp32"], choices=["fp32", "bf16"],
+                   help="join precision(s) to build with, one build each")
     ml = sub.add_parser("mlp")
     ml.add_argument("--n", type=int, default=200000)
     ml.add_argument("--queries", type=int, default=100000)
@@ -310,7 +316,7 @@ if __name__ == "__main__":
     if a.cmd == "mlp":
         mlp_case(a.n, a.queries)
     elif a.cmd == "build":
-        build_case(a.n, a.dim, a.data, a.K, a.L, a.check, a.S, a.trees, a.ml, a.iter)
+        build_case(a.n, a.dim, a.data, a.K, a.L, a.check, a.S, a.trees, a.ml, a.iter, a.precision)
     elif a.cmd == "knn":
         knn_case(a.n, a.nq, a.dim, a.k, a.data, a.screening, a.repeat)
     elif a.cmd == "table":

@@ -63,6 +63,7 @@ typedef struct efg_build_stats {
   uint64_t join_records;    /* neighbour-list insert candidates kept after the radius filter    */
   uint64_t merge_distances; /* leaf-merge distances of the initial graph                        */
   int32_t max_merge_depth;  /* on EFG_ERR_MERGE_LEVEL: deepest usable merge level               */
+  uint64_t join_fp32_nodes; /* BF16 build precision: node joins too large for one tensor-core tile */
 } efg_build_stats;
 
 /* Per-call search statistics. */
@@ -115,6 +116,16 @@ int efg_set_search_params(efg_index* idx, int epochs, int init_num, int extend_t
 #define EFG_PRECISION_BF16 1
 #define EFG_PRECISION_FP8 2  /* e4m3 copy with one FP32 scale per row (max|x| / 448); same re-rank */
 int efg_set_search_precision(efg_index* idx, int precision);
+/* Build precision: how the NN-descent join (base_index.hpp:328-371) computes its pair distances
+ * (no reference counterpart).  EFG_PRECISION_FP32, the default: FP32 rows on the CUDA cores.
+ * EFG_PRECISION_BF16: per node, one Gram tile of its new x (new + old) rows on the tensor cores from
+ * a BF16 copy of the base made at the start of each build, distance = |x|^2 + |y|^2 - 2 x.y; when
+ * BF16 holds every value one product per value, else three (hi + lo split, a relative error near
+ * 2^-17 of sum |x_k y_k|).  For integer data with squared norms below 2^23 (bytes up to 128
+ * dimensions) every distance, and so the graph, equals the FP32 build's; for other data pools can
+ * differ where distances tie within that error.  Nodes with more than 128 new or 256 new + old
+ * entries stay on the FP32 kernel (efg_build_stats.join_fp32_nodes). */
+int efg_set_build_precision(efg_index* idx, int precision);
 /* Bound on the nnexp search's per-query candidate buffer (no reference counterpart; the reference's
  * candidate vector grows without bound).  0, the default, sizes it for the worst case of one
  * expansion epoch, extend_to x graph degree, which cannot overflow.  A smaller bound needs less

@@ -426,10 +426,13 @@ int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms
   const size_t smem = join_smem(terms);
   if ((int64_t)smem > smem_max) return fail(EFG_ERR_ARG, "tensor-core join: shared memory");
   EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 1;
-  EFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_join_kernel, JTHREADS, smem));
-  per_sm = std::max(1, std::min(per_sm, 2));
-  tc_join_kernel<<<(unsigned)(sms * per_sm), JTHREADS, smem, s>>>(a);
+  // the whole shared-memory carveout, so that two CTAs fit an SM
+  EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared));
+  // two CTAs per SM (the occupancy calculator can answer one where two fit); the CTAs are
+  // persistent, so a second one that does not fit next to the first starts after it and finds the
+  // node counter spent
+  tc_join_kernel<<<(unsigned)(sms * 2), JTHREADS, smem, s>>>(a);
   EFG_CUDA(cudaGetLastError());
   return EFG_OK;
 }

@@ -552,7 +552,8 @@ struct WarpPool {
   uint32_t id[NS];  // with FLAG
 };
 
-// Next 32 records of a bucket in ascending (key, aux) order after `last`.
+// Next 32 records of a bucket in ascending (key, aux) order from `last` on (copies of `last`
+// included: the caller skips the ones it has applied).
 __device__ __forceinline__ K96 next_batch(const uint64_t* __restrict__ rk, const uint32_t* __restrict__ ra,
                                           uint32_t B, K96 last, bool first) {
   uint32_t lane = threadIdx.x & 31;
@@ -561,7 +562,7 @@ __device__ __forceinline__ K96 next_batch(const uint64_t* __restrict__ rk, const
     K96 x = k96_max();
     if (b + lane < B) {
       K96 y{rk[b + lane], ra[b + lane]};
-      if (first || lt(last, y)) x = y;
+      if (first || !lt(y, last)) x = y;
     }
     if (__all_sync(0xffffffffu, is_max(x))) continue;
     x = warp_sort32(x);
@@ -570,30 +571,78 @@ __device__ __forceinline__ K96 next_batch(const uint64_t* __restrict__ rk, const
   return run;
 }
 
-// One warp per target node: applies its records in ascending (dist, id, source, side) order
-// with Neighbor::insert / InsertIntoKnn semantics (base_index.hpp:37-61).  The reference rejects
-// a candidate whose id sits among the entries of equal distance; a pair's distance is the same
-// wherever the reference computes it, so that finds every repeat.  With any_dist a repeat is found
-// at any distance: the tensor-core join's distances can differ in the last bits from the FP32
-// ones a pool entry was inserted with, and an equal-distance test would let the id in twice.
-template <int NS>
-__global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_dist, const uint32_t* __restrict__ cnt,
-                             const uint64_t* __restrict__ rec_off, const uint64_t* __restrict__ rec_key,
-                             const uint32_t* __restrict__ rec_aux, float* __restrict__ pd,
-                             uint32_t* __restrict__ pid, uint32_t* __restrict__ Lc, float* __restrict__ radius,
-                             uint8_t* __restrict__ found, uint32_t* __restrict__ next_node) {
+// Ascending bitonic sort of Bp records (keys sk, aux sa; Bp a power of two >= 32) in shared
+// memory by one warp.
+__device__ __forceinline__ void warp_sort_smem(uint64_t* sk, uint32_t* sa, uint32_t Bp) {
   const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t k = 2; k <= Bp; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t t = lane; t < Bp / 2; t += 32) {
+        const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i + j;
+        const K96 x{sk[i], sa[i]}, y{sk[l], sa[l]};
+        if ((i & k) == 0 ? lt(y, x) : lt(x, y)) {
+          sk[i] = y.k;
+          sa[i] = y.a;
+          sk[l] = x.k;
+          sa[l] = x.a;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+constexpr uint32_t MERGE_WARPS = 4;  // warps per merge block
+
+// Lane of the smallest of the warp's 32 records (the lower lane on a tie), on every lane.
+__device__ __forceinline__ uint32_t warp_argmin(K96 x) {
+  uint32_t who = threadIdx.x & 31;
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    const K96 y = shfl_xor(x, m);
+    const uint32_t wy = __shfl_xor_sync(0xffffffffu, who, m);
+    if (lt(y, x) || (!lt(x, y) && wy < who)) {
+      x = y;
+      who = wy;
+    }
+  }
+  return who;
+}
+
+// One warp per target node: applies its records in ascending (dist, id, source, side) order,
+// every one of them (repeats of a record included), with Neighbor::insert / InsertIntoKnn
+// semantics (base_index.hpp:37-61).  The order comes from one of three sources:
+//   * up to msort records: sorted once in the warp's shared memory;
+//   * up to 32 x msort: runs of msort sorted in shared memory and written back in place, then
+//     merged 32 ways (lane l holds run l's head; 32 records of each run staged in shared memory);
+//   * more: pulled 32 at a time by scanning all of them.
+// The reference rejects a candidate whose id sits among the entries of equal distance; a pair's
+// distance is the same wherever the reference computes it, so that finds every repeat.  With
+// any_dist a repeat is found at any distance: the tensor-core join's distances can differ in the
+// last bits from the FP32 ones a pool entry was inserted with, and an equal-distance test would
+// let the id in twice.
+template <int NS>
+__global__ void __launch_bounds__(MERGE_WARPS * 32)
+    merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_dist, uint32_t msort,
+                 const uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off, uint64_t* __restrict__ rec_key,
+                 uint32_t* __restrict__ rec_aux, float* __restrict__ pd, uint32_t* __restrict__ pid,
+                 uint32_t* __restrict__ Lc, float* __restrict__ radius, uint8_t* __restrict__ found,
+                 uint32_t* __restrict__ next_node) {
+  extern __shared__ uint64_t merge_smem[];  // per warp: msort keys, then msort aux
+  const uint32_t lane = threadIdx.x & 31;
+  uint64_t* sk = merge_smem + (size_t)(threadIdx.x >> 5) * (msort + msort / 2);
+  uint32_t* sa = reinterpret_cast<uint32_t*>(sk + msort);
   for (;;) {  // nodes taken from a shared counter as warps come free (their record counts differ)
   uint32_t tt = 0;
   if (lane == 0) tt = atomicAdd(next_node, 1u);
   const uint64_t t = __shfl_sync(0xffffffffu, tt, 0);
   if (t >= n) return;
-  uint32_t B = cnt[t];
+  const uint32_t B = cnt[t];
   if (B == 0) continue;
-  const uint64_t* rk = rec_key + rec_off[t];
-  const uint32_t* ra = rec_aux + rec_off[t];
+  uint64_t* rk = rec_key + rec_off[t];
+  uint32_t* ra = rec_aux + rec_off[t];
   WarpPool<NS> pool;
-  uint64_t prow = t * P;
+  const uint64_t prow = t * P;
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
     uint32_t e = s * 32 + lane;
@@ -602,85 +651,175 @@ __global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_
   }
   uint32_t L = Lc[t];
   float rad = radius[t];
-  K96 last{0, 0};
-  bool first = true;
   bool rejected = false;
   K96 rej{0, 0};
-  while (true) {
-    K96 batch = next_batch(rk, ra, B, last, first);
-    first = false;
-    bool stop = false;
-    for (int u = 0; u < 32; ++u) {
-      K96 r = shfl_idx(batch, u);
-      if (is_max(r)) {
-        stop = true;
-        break;
-      }
-      last = r;
-      float d = key_dist(r.k);
-      uint32_t cand = key_id(r.k);
-      uint32_t rank;
-      if (d > rad) {  // rejected, and so is every later record
-        rejected = true;
-        rej = r;
-        stop = true;
-        break;
-      }
-      // i = entries of [0, L) with dist <= d
-      uint32_t i = 0, dup = 0;
-#pragma unroll
-      for (int s = 0; s < NS; ++s) {
-        uint32_t e = s * 32 + lane;
-        i += __popc(__ballot_sync(0xffffffffu, e < L && pool.d[s] <= d));
-      }
-#pragma unroll
-      for (int s = 0; s < NS; ++s) {
-        uint32_t e = s * 32 + lane;
-        dup |= __ballot_sync(0xffffffffu, (any_dist ? e < L : (e < i && pool.d[s] == d)) &&
-                                              (pool.id[s] & IDM) == cand);
-      }
-      if (dup) {
-        rank = L + 1;
-      } else {
-        // shift [i, L) up by one; entry L (<= P-1) receives entry L-1
-#pragma unroll
-        for (int s = NS - 1; s >= 0; --s) {
-          float ud = __shfl_up_sync(0xffffffffu, pool.d[s], 1);
-          uint32_t ui = __shfl_up_sync(0xffffffffu, pool.id[s], 1);
-          if (s > 0) {
-            float cd = __shfl_sync(0xffffffffu, pool.d[s > 0 ? s - 1 : 0], 31);
-            uint32_t ci = __shfl_sync(0xffffffffu, pool.id[s > 0 ? s - 1 : 0], 31);
-            if (lane == 0) {
-              ud = cd;
-              ui = ci;
-            }
-          }
-          uint32_t e = s * 32 + lane;
-          if (e > i && e <= L) {
-            pool.d[s] = ud;
-            pool.id[s] = ui;
-          } else if (e == i) {
-            pool.d[s] = d;
-            pool.id[s] = cand | FLAG;
-          }
-        }
-        rank = i;
-        if (L + 1 < P) {
-          ++L;
-        } else {
-          uint32_t e = L - 1;
-          float v = 0.f;
-#pragma unroll
-          for (int s = 0; s < NS; ++s) {
-            float w = __shfl_sync(0xffffffffu, pool.d[s], e & 31);
-            if ((uint32_t)s == e / 32) v = w;
-          }
-          rad = v;
-        }
-      }
-      if ((r.a & 1u) == 0 && rank < check_k && lane == 0) found[r.a >> 1] = 1;
+
+  // Applies record r; true when r is rejected (every later record is too).
+  auto apply = [&](const K96 r) -> bool {
+    const float d = key_dist(r.k);
+    const uint32_t cand = key_id(r.k);
+    uint32_t rank;
+    if (d > rad) {
+      rejected = true;
+      rej = r;
+      return true;
     }
-    if (stop) break;
+    // i = entries of [0, L) with dist <= d
+    uint32_t i = 0, dup = 0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      uint32_t e = s * 32 + lane;
+      i += __popc(__ballot_sync(0xffffffffu, e < L && pool.d[s] <= d));
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      uint32_t e = s * 32 + lane;
+      dup |= __ballot_sync(0xffffffffu,
+                           (any_dist ? e < L : (e < i && pool.d[s] == d)) && (pool.id[s] & IDM) == cand);
+    }
+    if (dup) {
+      rank = L + 1;
+    } else {
+      // shift [i, L) up by one; entry L (<= P-1) receives entry L-1
+#pragma unroll
+      for (int s = NS - 1; s >= 0; --s) {
+        float ud = __shfl_up_sync(0xffffffffu, pool.d[s], 1);
+        uint32_t ui = __shfl_up_sync(0xffffffffu, pool.id[s], 1);
+        if (s > 0) {
+          float cd = __shfl_sync(0xffffffffu, pool.d[s > 0 ? s - 1 : 0], 31);
+          uint32_t ci = __shfl_sync(0xffffffffu, pool.id[s > 0 ? s - 1 : 0], 31);
+          if (lane == 0) {
+            ud = cd;
+            ui = ci;
+          }
+        }
+        uint32_t e = s * 32 + lane;
+        if (e > i && e <= L) {
+          pool.d[s] = ud;
+          pool.id[s] = ui;
+        } else if (e == i) {
+          pool.d[s] = d;
+          pool.id[s] = cand | FLAG;
+        }
+      }
+      rank = i;
+      if (L + 1 < P) {
+        ++L;
+      } else {
+        uint32_t e = L - 1;
+        float v = 0.f;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+          float w = __shfl_sync(0xffffffffu, pool.d[s], e & 31);
+          if ((uint32_t)s == e / 32) v = w;
+        }
+        rad = v;
+      }
+    }
+    if ((r.a & 1u) == 0 && rank < check_k && lane == 0) found[r.a >> 1] = 1;
+    return false;
+  };
+
+  const uint32_t runs = (B + msort - 1) / msort;
+  if (runs <= 32) {
+    // sort each run of msort records in shared memory (a single run stays there)
+    for (uint32_t q = 0; q < runs; ++q) {
+      const uint32_t b0 = q * msort, len = min(msort, B - b0);
+      uint32_t Bp = 32;
+      while (Bp < len) Bp <<= 1;
+      for (uint32_t b = lane; b < Bp; b += 32) {
+        sk[b] = b < len ? rk[b0 + b] : ~0ULL;
+        sa[b] = b < len ? ra[b0 + b] : 0xffffffffu;
+      }
+      __syncwarp();
+      warp_sort_smem(sk, sa, Bp);
+      if (runs > 1) {
+        for (uint32_t b = lane; b < len; b += 32) {
+          rk[b0 + b] = sk[b];
+          ra[b0 + b] = sa[b];
+        }
+        __syncwarp();
+      }
+    }
+    if (runs == 1) {
+      bool stop = false;
+      for (uint32_t base = 0; base < B && !stop; base += 32) {
+        const K96 batch = base + lane < B ? K96{sk[base + lane], sa[base + lane]} : k96_max();
+        const uint32_t m = min(32u, B - base);
+        for (uint32_t u = 0; u < m; ++u)
+          if (apply(shfl_idx(batch, u))) {
+            stop = true;
+            break;
+          }
+      }
+    } else {
+      // 32-way merge: lane q holds run q's head; run q's records [ws, ws + SD) staged at
+      // sk/sa[SD q ..]
+      const uint32_t SD = msort / 32;
+      const uint32_t my_len = lane < runs ? min(msort, B - lane * msort) : 0;
+      uint32_t at = 0, ws = 0;  // lane q: next record of run q, first staged record of run q
+      for (uint32_t q = 0; q < runs; ++q) {
+        const uint32_t len = min(msort, B - q * msort);
+        if (lane < SD && lane < len) {
+          sk[SD * q + lane] = rk[q * msort + lane];
+          sa[SD * q + lane] = ra[q * msort + lane];
+        }
+      }
+      __syncwarp();
+      for (;;) {
+        const K96 head = at < my_len ? K96{sk[SD * lane + at - ws], sa[SD * lane + at - ws]} : k96_max();
+        const uint32_t w = warp_argmin(head);
+        const K96 r = shfl_idx(head, w);
+        if (is_max(r)) break;
+        if (apply(r)) break;
+        if (lane == w) ++at;
+        const uint32_t wat = __shfl_sync(0xffffffffu, at, w), wws = __shfl_sync(0xffffffffu, ws, w);
+        const uint32_t wlen = __shfl_sync(0xffffffffu, my_len, w);
+        if (wat == wws + SD && wat < wlen) {  // run w's staged records are spent: stage the next SD
+          __syncwarp();
+          if (lane < SD && wat + lane < wlen) {
+            sk[SD * w + lane] = rk[w * msort + wat + lane];
+            sa[SD * w + lane] = ra[w * msort + wat + lane];
+          }
+          __syncwarp();
+          if (lane == w) ws = wat;
+        }
+      }
+    }
+  } else {
+    // scanning: the next 32 records from the last applied one on, copies of it included
+    K96 last{0, 0};
+    uint32_t last_n = 0;  // copies of `last` applied so far
+    bool first = true, stop = false;
+    while (!stop) {
+      const K96 batch = next_batch(rk, ra, B, last, first);
+      first = false;
+      uint32_t skip = last_n;  // the batch starts with every copy of `last`
+      bool applied = false;
+      for (int u = 0; u < 32; ++u) {
+        const K96 r = shfl_idx(batch, u);
+        if (is_max(r)) {
+          stop = true;
+          break;
+        }
+        if (skip) {
+          --skip;
+          continue;
+        }
+        applied = true;
+        if (last_n && r.k == last.k && r.a == last.a) {
+          ++last_n;
+        } else {
+          last = r;
+          last_n = 1;
+        }
+        if (apply(r)) {
+          stop = true;
+          break;
+        }
+      }
+      if (!applied) break;  // a batch of nothing but applied copies (more than 32 repeats)
+    }
   }
   if (rejected && P < check_k) {
     // every record from `rej` on was rejected with rank P < check_k
@@ -1042,19 +1181,23 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
                                              S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.rec_off64.p,
                                              S.cursor.p, S.rec_key.p, S.rec_aux.p, jctr.p + 1);
   EFG_CUDA(cudaGetLastError());
-  const unsigned mgrid = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * 8);
-  if (S.P <= 32)
-    merge_kernel<1><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
-                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
-  else if (S.P <= 64)
-    merge_kernel<2><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
-                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
-  else if (S.P <= 128)
-    merge_kernel<4><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
-                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
-  else
-    merge_kernel<8><<<mgrid, 256, 0, s>>>(n, S.P, bp.check_k, tc, S.cnt.p, S.rec_off64.p, S.rec_key.p, S.rec_aux.p,
-                                          S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
+  // merge: a warp per target node; records of up to msort per node sorted in shared memory
+  const uint32_t msort = S.P > 64 ? 1024 : 256;
+  const size_t msmem = (size_t)MERGE_WARPS * msort * 12;
+  auto launch_merge = [&](auto kern) -> int {
+    EFG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem));
+    int per = 1;
+    EFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, MERGE_WARPS * 32, msmem));
+    const unsigned grid = (unsigned)std::min<uint64_t>(blocks_for(n * 32, MERGE_WARPS * 32),
+                                                       (uint64_t)sms * std::max(per, 1));
+    kern<<<grid, MERGE_WARPS * 32, msmem, s>>>(n, S.P, bp.check_k, tc, msort, S.cnt.p, S.rec_off64.p, S.rec_key.p,
+                                               S.rec_aux.p, S.pd.p, S.pid.p, S.Lc.p, S.radius.p, S.found.p, jctr.p + 2);
+    return EFG_OK;
+  };
+  if (S.P <= 32) EFG_TRY(launch_merge(merge_kernel<1>));
+  else if (S.P <= 64) EFG_TRY(launch_merge(merge_kernel<2>));
+  else if (S.P <= 128) EFG_TRY(launch_merge(merge_kernel<4>));
+  else EFG_TRY(launch_merge(merge_kernel<8>));
   EFG_CUDA(cudaGetLastError());
   // ---- update
   update_range_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, S.P, bp.S, S.pd.p, S.pid.p, S.Lc.p, S.Range.p,

@@ -177,6 +177,22 @@ def run_gpu(args):
         build_s.append(time.perf_counter() - t0)
     bst = idx.build_stats()
     graph = idx.graph()
+    # the same build with the join's pair distances on the tensor cores (exact on byte data: the
+    # graph must come out identical)
+    idx_t = E.Index.from_device(X.data_ptr(), args.n, 128, 128, E.IndexParams(**GRAPH))
+    idx_t.set_build_precision("bf16")
+    tc_build_s = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        idx_t.build_index()
+        torch.cuda.synchronize()
+        tc_build_s.append(time.perf_counter() - t0)
+    tst = idx_t.build_stats()
+    tc_build = {"graph_build_s": round(min(tc_build_s), 4), "refine_ms": round(tst.refine_ms, 2),
+                "identical_graph": bool(np.array_equal(idx_t.graph(), graph)),
+                "join": "tensor cores (tcgen05), one product per value (BF16 holds byte data)"}
+    idx_t.close()
     # the same build from host rows, as the reference's buildIndex is called: the index's copy of the
     # 512 MB base to the device is inside the timed region
     torch.cuda.synchronize()
@@ -333,7 +349,8 @@ def run_gpu(args):
                   "graph_build_host_input_s": round(host_build_s, 4),
                   "trees_ms": round(bst.trees_ms, 2), "init_ms": round(bst.init_ms, 2),
                   "refine_ms": round(bst.refine_ms, 2), "join_pairs": int(bst.join_pairs),
-                  "graph_recall@10": round(graph_recall, 4), "search_trees16_s": round(trees_s, 4)},
+                  "graph_recall@10": round(graph_recall, 4), "search_trees16_s": round(trees_s, 4),
+                  "tensor_core_join": tc_build},
         "e2e": {"value": round(f32["e2e"], 1), "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(nq * 10 * 4)},
         "roofline": roofline(f32),
@@ -630,6 +647,17 @@ def measure_precision_960(E, args, hbm, peak_kind):
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     bst = idx.build_stats()
+    # the same graph build with the join's pair distances on the tensor cores (hi + lo products)
+    idx_t = E.Index.from_device(X.data_ptr(), n, d, d, E.IndexParams(**P960_GRAPH))
+    idx_t.set_build_precision("bf16")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx_t.build_index()
+    torch.cuda.synchronize()
+    tc_build_s = time.perf_counter() - t0
+    tst = idx_t.build_stats()
+    tc_graph = idx_t.graph()
+    idx_t.close()
     # exact 100-NN of the queries (tensor-core screening, hi + lo split on this float data)
     gt = torch.zeros((nq, k), dtype=torch.int32, device="cuda")
     E.brute_force_knn_device(X.data_ptr(), n, d, d, Q.data_ptr(), nq, d, k, gt.data_ptr())
@@ -646,6 +674,9 @@ def measure_precision_960(E, args, hbm, peak_kind):
     graph = idx.graph()
     graph_recall = float(np.mean([len(set(graph[r].tolist()) & set([v for v in g101[i] if v != r][:k])) / k
                                   for i, r in enumerate(rows)]))
+    tc_recall = float(np.mean([len(set(tc_graph[r].tolist()) & set([v for v in g101[i] if v != r][:k])) / k
+                               for i, r in enumerate(rows)]))
+    del tc_graph
     out = torch.zeros((nq, k), dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -723,6 +754,10 @@ def measure_precision_960(E, args, hbm, peak_kind):
             "build_phases_ms": {"trees": round(bst.trees_ms, 1), "init": round(bst.init_ms, 1),
                                 "refine": round(bst.refine_ms, 1)},
             "join_pairs": int(bst.join_pairs), "graph_recall@100": round(graph_recall, 4),
+            "tensor_core_join": {"graph_build_s": round(tc_build_s, 3), "refine_ms": round(tst.refine_ms, 1),
+                                 "graph_recall@100": round(tc_recall, 4),
+                                 "nodes_larger_than_a_tile": int(tst.join_large_nodes),
+                                 "join": "tensor cores (tcgen05), hi + lo BF16 split (3 products per value)"},
             "operating_point": {"epochs": point[0], "pool": point[1], "extend": point[2]}, "ladder": ladder,
             "exact_knn": knn_line(kst, "hi + lo BF16 split (3 products per value)"),
             **per}

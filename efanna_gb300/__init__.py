@@ -43,7 +43,7 @@ class BuildStats(C.Structure):
     _fields_ = [("trees_ms", C.c_double), ("init_ms", C.c_double), ("refine_ms", C.c_double),
                 ("total_ms", C.c_double), ("join_pairs", C.c_uint64), ("join_records", C.c_uint64),
                 ("merge_distances", C.c_uint64), ("max_merge_depth", C.c_int32),
-                ("join_fp32_nodes", C.c_uint64)]
+                ("join_large_nodes", C.c_uint64)]
 
 
 class SearchStats(C.Structure):

@@ -16,8 +16,11 @@
 //     warps of each TMEM lane quarter taking alternate 32-column groups) into shared memory, then
 //     walk those entries' pairs in pair-array order, one pair per thread: distance
 //     ||x||^2 + ||y||^2 - 2 x.y, then the join's record step -- the same per-pair array, per-target
-//     counts and `found` flags as the FP32 join kernel, which covers the nodes too large for one
-//     tile (more than 128 new entries or 256 rows; they are listed for it here).
+//     counts and `found` flags as the FP32 join kernel.
+//   * Nodes too large for one tile (more than 128 new entries or 256 rows) are listed and scored by
+//     a second launch, tile by tile: a block of up to 128 new entries (the tile's first rows) with a
+//     chunk of the candidates after the block; the block's first chunk also covers the pairs within
+//     the block.  Each row's pairs in a tile are consecutive slots of the node's pair array.
 //   * When BF16 holds every value of the base, one product per value; with integer values and
 //     squared norms below 2^23 (byte data up to 128 dimensions) every sum is exact, so the distances
 //     equal the FP32 join's and the graph is identical.  Other data take the hi + lo split
@@ -46,6 +49,7 @@ constexpr uint32_t JTHREADS = 64 + JRT;
 constexpr uint32_t JPROD = JTHREADS - 32;  // row-gathering threads (every warp but the MMA warp)
 constexpr uint32_t DLD = JR + 1;      // row stride of the Gram rows in shared memory (conflict-free)
 constexpr uint32_t JCH = 32;          // consecutive nodes taken from the counter at a time
+constexpr uint32_t NONE = 0xffffffffu;
 
 struct JoinArgs {
   const __nv_bfloat16 *hi, *lo;  // BF16 rows of W values (lo only read when terms = 3)
@@ -57,10 +61,11 @@ struct JoinArgs {
   uint32_t* cnt;
   uint8_t* found;
   uint32_t* next_node;  // node counter (chunks of JCH nodes)
-  uint32_t* big;        // nodes left to the FP32 kernel: big[0] their count, then their ids
+  uint32_t* big;        // nodes larger than one tile: big[0] their count, then their ids
   int* err;
   uint64_t n;
   uint32_t W, cap, P, check_k, kblocks, terms, nstages, stage_bytes;
+  uint32_t big_mode;  // 1: the listed nodes, each as tiles of up to 128 new rows x a chunk of candidates
 };
 
 // Offset of new entry p's first pair within the node's pairs (nn new, no old entries).
@@ -88,6 +93,10 @@ __global__ void __launch_bounds__(JTHREADS, 2)
   __shared__ float norm_sh[JR];
   __shared__ uint32_t tmem_base_sh, i0_sh, chn_sh, chpos_sh, tn_sh, nsum_sh, tsum_sh;
   __shared__ int abort_sh, rec_fail_sh, bad_sh;
+  // big mode: the node (its id, list lengths, pair offset), the next tile's new block and candidate
+  // chunk start, whether it is the block's first (the one with the triangle), and the tile taken
+  __shared__ uint32_t bm_node, bm_nn, bm_no, bm_a0, bm_c0, bm_first, bm_tri, bm_tc0, bm_ch;
+  __shared__ uint64_t bm_po;
   const uint32_t raw = smem_addr(smem_raw);
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
   const uint32_t sbase = raw + pad;
@@ -104,6 +113,7 @@ __global__ void __launch_bounds__(JTHREADS, 2)
     abort_sh = 0;
     chn_sh = 0;
     chpos_sh = 0;
+    bm_node = NONE;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -123,6 +133,67 @@ __global__ void __launch_bounds__(JTHREADS, 2)
 
   for (;;) {
     __syncthreads();  // the previous tile's rows and entry arrays are no longer read
+    if (a.big_mode) {
+      // ---------------------------------------------------------- big mode: the next tile of a listed node
+      if (threadIdx.x == 0) {
+        uint32_t tn = 0;
+        bad_sh = 0;
+        rec_fail_sh = 0;
+        while (!*abort_flag) {
+          if (bm_node == NONE) {
+            const uint32_t k = atomicAdd(a.next_node, 1u);
+            if (k >= a.big[0]) break;
+            const uint32_t i = a.big[1 + k];
+            bm_node = i;
+            bm_nn = a.new_cnt[i];
+            bm_no = a.old_cnt[i];
+            bm_po = a.pair_off[i];
+            bm_a0 = 0;
+            bm_c0 = min(JM, bm_nn);
+            bm_first = 1;
+          }
+          const uint32_t nn = bm_nn, T = nn + bm_no, A = min(JM, nn - bm_a0);
+          if (bm_c0 < T || (bm_first && A > 1)) {  // a tile with pairs
+            const uint32_t ch = min(JR - A, T - bm_c0);
+            bm_tri = bm_first;
+            bm_tc0 = bm_c0;
+            bm_ch = ch;
+            bm_c0 += ch;
+            bm_first = 0;
+            nsum_sh = A;
+            tsum_sh = A + ch;
+            tn = 1;
+            break;
+          }
+          bm_a0 += A;  // the next block of new entries, or the next node
+          if (bm_a0 >= nn) bm_node = NONE;
+          else {
+            bm_c0 = min(bm_a0 + JM, nn);
+            bm_first = 1;
+          }
+        }
+        tn_sh = tn;
+      }
+      __syncthreads();
+      if (tn_sh == 0) break;
+      const uint32_t A = nsum_sh, nn = bm_nn, no = bm_no, a0 = bm_a0, c0 = bm_tc0, tri = bm_tri;
+      const uint64_t i = bm_node;
+      for (uint32_t b = threadIdx.x; b < tsum_sh; b += JTHREADS) {
+        const uint32_t c = b < A ? a0 + b : c0 + (b - A);  // entry of the node's lists (new, then old)
+        uint32_t r = c < nn ? a.new_ids[i * a.cap + c] : a.old_ids[i * a.cap + c - nn];
+        if (r >= a.n) {
+          bad_sh = 1;
+          r = 0;
+        }
+        rows_sh[b] = r;
+        norm_sh[b] = a.xnorm[r];
+        if (b < A) {
+          const uint32_t pe = a0 + b;
+          rnode[b] = 0;
+          rstart[b] = bm_po + pair_row(nn, no, pe) + (tri ? 0 : c0 - pe - 1);
+        }
+      }
+    } else {
     if (chpos_sh >= chn_sh) {  // the chunk is packed: the next JCH nodes
       if (threadIdx.x == 0) i0_sh = *abort_flag ? (uint32_t)a.n : atomicAdd(a.next_node, JCH);
       __syncthreads();
@@ -180,11 +251,9 @@ __global__ void __launch_bounds__(JTHREADS, 2)
       rec_fail_sh = 0;
     }
     __syncthreads();
-    const uint32_t tn = tn_sh;
-    if (tn == 0) continue;
-    const uint32_t Ns = nsum_sh, Ts = tsum_sh, Tpad = (Ts + 15) & ~15u;
+    if (tn_sh == 0) continue;
     const uint64_t i0 = i0_sh;
-    for (uint32_t j = warp; j < tn; j += JTHREADS / 32) {  // a warp per tile node
+    for (uint32_t j = warp; j < tn_sh; j += JTHREADS / 32) {  // a warp per tile node
       const uint32_t sl = tslot[j], nn = nn_ch[sl], no = no_ch[sl];
       const uint64_t i = i0 + sl;
       for (uint32_t e = lane; e < nn + no; e += 32) {
@@ -202,7 +271,10 @@ __global__ void __launch_bounds__(JTHREADS, 2)
         }
       }
     }
+    }
     __syncthreads();
+    const uint32_t Ns = nsum_sh, Ts = tsum_sh, Tpad = (Ts + 15) & ~15u;
+    const uint64_t i0 = i0_sh;  // (packed tiles) the chunk's first node
     if (bad_sh) {
       if (threadIdx.x == 0) atomicOr(a.err, 4);
       continue;
@@ -285,8 +357,12 @@ __global__ void __launch_bounds__(JTHREADS, 2)
           const uint32_t r = r0 + lane;
           uint32_t v = 0;
           if (r < Ns) {
-            const uint32_t j = rnode[r], sl = tslot[j];
-            v = nn_ch[sl] + no_ch[sl] - 1 - (r - tnb[j]);
+            if (a.big_mode) {
+              v = (bm_tri ? Ns - r - 1 : 0) + bm_ch;
+            } else {
+              const uint32_t j = rnode[r], sl = tslot[j];
+              v = nn_ch[sl] + no_ch[sl] - 1 - (r - tnb[j]);
+            }
           }
 #pragma unroll
           for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -323,14 +399,32 @@ __global__ void __launch_bounds__(JTHREADS, 2)
           uint32_t r = q0;
           for (uint32_t u = cum[q0] + t; u < u1; u += JRT) {
             while (u >= cum[r + 1]) ++r;
-            const uint32_t j = rnode[r], sl = tslot[j], nn = nn_ch[sl];
-            const uint32_t off = u - cum[r], cl = r - tnb[j] + 1 + off;  // candidate within the node's lists
-            const uint32_t bc = cl < nn ? tnb[j] + cl : tob[j] + (cl - nn);
+            const uint32_t off = u - cum[r];
+            uint32_t bc;     // the candidate's row in the tile
+            bool cand_new;   // the candidate is a new entry
+            uint64_t node;
+            if (a.big_mode) {
+              const uint32_t tl = bm_tri ? Ns - r - 1 : 0;  // the row's pairs within the new block
+              if (off < tl) {
+                bc = r + 1 + off;
+                cand_new = true;
+              } else {
+                bc = Ns + (off - tl);
+                cand_new = bm_tc0 + (off - tl) < bm_nn;
+              }
+              node = bm_node;
+            } else {
+              const uint32_t j = rnode[r], sl = tslot[j], nn = nn_ch[sl];
+              const uint32_t cl = r - tnb[j] + 1 + off;  // candidate within the node's lists
+              bc = cl < nn ? tnb[j] + cl : tob[j] + (cl - nn);
+              cand_new = cl < nn;
+              node = i0 + sl;
+            }
             const float dot = gram[(r - q0) * DLD + bc];
             const float d = fmaxf(fmaf(-2.f, dot, norm_sh[r] + norm_sh[bc]), 0.f);
-            if (join_lane_record<0>(i0 + sl, rows_sh[r], rows_sh[bc], cl < nn, d, rstart[r] + off, a.P, a.check_k,
+            if (join_lane_record<0>(node, rows_sh[r], rows_sh[bc], cand_new, d, rstart[r] + off, a.P, a.check_k,
                                     a.bound, a.pairdist, a.cnt, nullptr, nullptr, nullptr, nullptr))
-              a.found[i0 + sl] = 1;
+              a.found[node] = 1;
           }
           rec_sync();  // the Gram rows are overwritten by the next 32 entries
         }
@@ -383,14 +477,16 @@ int tc_join_prepare(const float* base, uint64_t n, uint32_t dim, uint32_t ld, __
   return EFG_OK;
 }
 
-// Join pass 0 on the tensor cores for every node that fits one tile; the others are listed in big
-// (big[0] their count, then their ids) for the FP32 kernel.  next_node, big[0] and *err must be
-// zero on entry.  terms: 1 (BF16 holds the base) or 3 (hi + lo products).
+// Join pass 0 on the tensor cores.  big_mode 0: every node that fits one tile, packed several to a
+// tile; the others are listed in big (big[0] their count, then their ids), which must be zero on
+// entry.  big_mode 1: the listed nodes, each as tiles of up to 128 new entries x up to 256 rows.
+// next_node (a node counter of each launch) and *err must be zero on entry.  terms: 1 (BF16 holds
+// the base) or 3 (hi + lo products).
 int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms, uint64_t n, uint32_t dim,
             uint32_t terms, uint32_t cap, uint32_t P, uint32_t check_k, const uint32_t* new_ids,
             const uint32_t* new_cnt, const uint32_t* old_ids, const uint32_t* old_cnt, const uint64_t* pair_off,
             const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* next_node, uint32_t* big,
-            int* err, cudaStream_t s) {
+            int big_mode, int* err, cudaStream_t s) {
   if (terms != 1 && terms != 3) return fail(EFG_ERR_ARG, "tensor-core join: terms must be 1 or 3");
   const uint32_t W = (dim + 63) / 64 * 64;
   int dev = 0, sms = 148, smem_max = 0;
@@ -422,6 +518,7 @@ int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms
   a.terms = terms;
   a.nstages = terms == 1 ? 2 : 1;
   a.stage_bytes = (terms == 1 ? 1u : 2u) * JPART;
+  a.big_mode = big_mode ? 1u : 0u;
   // about 97 KB per CTA: two fit on an SM, three do not (two 256-column accumulators fill TMEM)
   const size_t smem = join_smem(terms);
   if ((int64_t)smem > smem_max) return fail(EFG_ERR_ARG, "tensor-core join: shared memory");

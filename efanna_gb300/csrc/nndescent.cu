@@ -1138,7 +1138,7 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   const unsigned jgrid1 = (unsigned)std::min<uint64_t>(blocks_for(n * 32, 256), (uint64_t)sms * std::max(per1, 1));
   const bool tc = idx->build_precision == EFG_PRECISION_BF16;
   if (tc) {
-    // pass 0 on the tensor cores; nodes too large for one tile go to the FP32 kernel's node list
+    // pass 0 on the tensor cores: nodes that fit one tile packed together, then the larger ones
     if (!S.jterms) {
       const uint64_t W = (idx->dim + 63) / 64 * 64;
       EFG_TRY(S.jhi.reserve(n * W));
@@ -1154,19 +1154,21 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
     }
     EFG_CUDA(cudaMemsetAsync(S.jflag.p + 1, 0, 4, s));
     EFG_CUDA(cudaMemsetAsync(S.jbig.p, 0, 4, s));
-    EFG_TRY(tc_join(S.jhi.p, S.jlo.p, S.jnorm.p, n, idx->dim, S.jterms, S.cap, S.P, bp.check_k, S.new_ids.p,
-                    S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p, S.found.p,
-                    jctr.p, S.jbig.p, S.jflag.p + 1, s));
+    for (int big_mode = 0; big_mode < 2; ++big_mode)  // the nodes of one tile, then the larger ones
+      EFG_TRY(tc_join(S.jhi.p, S.jlo.p, S.jnorm.p, n, idx->dim, S.jterms, S.cap, S.P, bp.check_k, S.new_ids.p,
+                      S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
+                      S.found.p, big_mode ? jctr.p + 3 : jctr.p, S.jbig.p, big_mode, S.jflag.p + 1, s));
+  } else {
+    join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
+                                            S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
+                                            S.found.p, jctr.p, nullptr);
+    EFG_CUDA(cudaGetLastError());
   }
-  join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
-                                          S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
-                                          S.found.p, tc ? jctr.p + 3 : jctr.p, tc ? S.jbig.p : nullptr);
-  EFG_CUDA(cudaGetLastError());
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, tmp64.p, n);
   EFG_TRY(device_scan<uint64_t>(tmp64.p, n, S.rec_off64.p, S.scan64.p, s));
   uint64_t nrec = 0;
   EFG_CUDA(cudaMemcpyAsync(&nrec, S.rec_off64.p + n, 8, cudaMemcpyDeviceToHost, s));
-  int jstat[2] = {0, 0};  // tensor-core join: error word, nodes left to the FP32 kernel
+  int jstat[2] = {0, 0};  // tensor-core join: error word, nodes larger than one tile
   if (tc) {
     EFG_CUDA(cudaMemcpyAsync(&jstat[0], S.jflag.p + 1, 4, cudaMemcpyDeviceToHost, s));
     EFG_CUDA(cudaMemcpyAsync(&jstat[1], S.jbig.p, 4, cudaMemcpyDeviceToHost, s));
@@ -1174,7 +1176,7 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaStreamSynchronize(s));
   if (jstat[0] & 4) return fail(EFG_ERR_ARG, "tensor-core join: a join list holds an id >= n");
   if (jstat[0]) return fail(EFG_ERR_DEVICE_LIMIT, "tensor-core join: a wait ran out on the device");
-  idx->bstats.join_fp32_nodes += (uint32_t)jstat[1];
+  idx->bstats.join_large_nodes += (uint32_t)jstat[1];
   EFG_TRY(S.rec_key.reserve(nrec + 1));
   EFG_TRY(S.rec_aux.reserve(nrec + 1));
   join_records_kernel<<<jgrid1, 256, 0, s>>>(n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p, S.old_ids.p,

@@ -157,10 +157,10 @@ def build_case(n: int, dim: int, data: str, K: int, L: int, check: int, S: int, 
         rec = np.mean([len(set(g[r].tolist()) & set([v for v in gtn[i] if v != r][:K])) / K
                        for i, r in enumerate(rows)])
         print("build %s %d x %d K=%d L=%d check=%d S=%d trees=%d ml=%d iter=%d join %s: data %.1f s, build %.3f s "
-              "(trees %.1f ms, init %.1f ms, refine %.1f ms), join pairs %d, records %d, FP32-kernel nodes %d; "
+              "(trees %.1f ms, init %.1f ms, refine %.1f ms), join pairs %d, records %d, nodes larger than a tile %d; "
               "graph recall@%d (2000 rows) %.4f"
               % (data, n, dim, K, L, check, S, trees, ml, iters, prec, gen_s, build_s, st.trees_ms, st.init_ms,
-                 st.refine_ms, st.join_pairs, st.join_records, st.join_fp32_nodes, K, rec), flush=True)
+                 st.refine_ms, st.join_pairs, st.join_records, st.join_large_nodes, K, rec), flush=True)
         idx.close()
 
 

@@ -63,7 +63,7 @@ typedef struct efg_build_stats {
   uint64_t join_records;    /* neighbour-list insert candidates kept after the radius filter    */
   uint64_t merge_distances; /* leaf-merge distances of the initial graph                        */
   int32_t max_merge_depth;  /* on EFG_ERR_MERGE_LEVEL: deepest usable merge level               */
-  uint64_t join_fp32_nodes; /* BF16 build precision: node joins too large for one tensor-core tile */
+  uint64_t join_large_nodes; /* BF16 build precision: node joins larger than one tensor-core tile */
 } efg_build_stats;
 
 /* Per-call search statistics. */
@@ -123,8 +123,9 @@ int efg_set_search_precision(efg_index* idx, int precision);
  * BF16 holds every value one product per value, else three (hi + lo split, a relative error near
  * 2^-17 of sum |x_k y_k|).  For integer data with squared norms below 2^23 (bytes up to 128
  * dimensions) every distance, and so the graph, equals the FP32 build's; for other data pools can
- * differ where distances tie within that error.  Nodes with more than 128 new or 256 new + old
- * entries stay on the FP32 kernel (efg_build_stats.join_fp32_nodes). */
+ * differ where distances tie within that error.  Several nodes share one tile of 128 new x 256
+ * rows; a node with more is scored as blocks of its new entries x chunks of its candidates
+ * (efg_build_stats.join_large_nodes counts them). */
 int efg_set_build_precision(efg_index* idx, int precision);
 /* Bound on the nnexp search's per-query candidate buffer (no reference counterpart; the reference's
  * candidate vector grows without bound).  0, the default, sizes it for the worst case of one

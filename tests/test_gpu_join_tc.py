@@ -4,7 +4,8 @@ the FP32 join.
 On byte-valued data up to 128 dimensions every Gram value, norm and distance is an integer below
 2^24, so the tensor-core join must leave exactly the oracle's state after every iteration (the FP32
 join's is pinned to it by test_gpu_parity) and build the identical graph.  Nodes too large for one
-tile (more than 128 new entries or 256 rows) stay on the FP32 kernel; one case here has many.  On
+tile (more than 128 new entries or 256 rows) are scored tile by tile in a second launch; one case
+here has many.  On
 real-valued data (hi + lo products) the graph may differ where distances tie within the split's
 error; its recall against exact neighbours must stay within 0.005 of the FP32 build's.
 """
@@ -60,9 +61,9 @@ def test_tc_join_iterations_match_oracle(efg, oracle_lib, n, d, params):
 
 
 def test_tc_join_oversized_lists_match_oracle(efg, oracle_lib):
-    """Nodes beyond one tile (more than 128 new entries, or more than 256 rows) go to the FP32
-    kernel's node list; lists that large do not arise at test sizes, so some nodes of a real
-    initial state get long random lists (any lists are a valid join input)."""
+    """Nodes beyond one tile (more than 128 new entries, or more than 256 rows) are scored as
+    blocks of new entries x chunks of candidates; lists that large do not arise at test sizes, so
+    some nodes of a real initial state get long random lists (any lists are a valid join input)."""
     O = oracle_lib
     n, d = 3000, 32
     params = dict(trees=4, merge_level=3, epochs=1, check=40, L=30, K=10, S=10, reverse_cap=400)
@@ -106,7 +107,7 @@ def test_tc_join_graph_identical_on_byte_data(efg, d):
     assert np.array_equal(a.graph(), b.graph())
     sa, sb = a.build_stats(), b.build_stats()
     assert sa.join_pairs == sb.join_pairs and sa.join_records == sb.join_records
-    assert sa.join_fp32_nodes == 0 and sb.join_fp32_nodes == 0
+    assert sa.join_large_nodes == 0 and sb.join_large_nodes == 0
 
 
 def test_tc_join_float_data_recall(efg):

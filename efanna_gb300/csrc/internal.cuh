@@ -174,16 +174,16 @@ int brute_force_knn_tc(const float* base, uint64_t n, uint32_t dim, uint32_t ld,
                        cudaStream_t s, int force_split = 0);
 // join_tc.cu: the NN-descent join's pass 0 on the tensor cores.  tc_join_prepare converts the base
 // to BF16 hi / lo rows of round_up(dim, 64) values with FP32 norms and sets *inexact when some lo is
-// not zero; tc_join (big_mode 0) scores every node that fits one tile (<= 128 new, <= 256 rows) and
-// lists the others in big (big[0] their count), which tc_join with big_mode 1 then scores tile by
-// tile; err is set when a wait ran out or a list holds an id >= n.
+// not zero; tc_join scores every node in three launches (tiles of 128 rows over all nodes, tiles of
+// 256 rows over the nodes listed in mid, the nodes listed in big tile by tile; counters: three node
+// counters); err is set when a wait ran out or a list holds an id >= n.
 int tc_join_prepare(const float* base, uint64_t n, uint32_t dim, uint32_t ld, __nv_bfloat16* hi, __nv_bfloat16* lo,
                     float* norms, int* inexact, cudaStream_t s);
 int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms, uint64_t n, uint32_t dim,
             uint32_t terms, uint32_t cap, uint32_t P, uint32_t check_k, const uint32_t* new_ids,
             const uint32_t* new_cnt, const uint32_t* old_ids, const uint32_t* old_cnt, const uint64_t* pair_off,
-            const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* next_node, uint32_t* big,
-            int big_mode, int* err, cudaStream_t s);
+            const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* counters, uint32_t* mid,
+            uint32_t* big, int* err, cudaStream_t s);
 // mlp_tc.cu: the learned form's dense layers on the tensor cores, C = act(A W^T + bias) (A: M x K,
 // W: N x K, BF16 row-major; C FP32 and / or Cb BF16, M x N); EFG_ERR_ARG when the shape does not fit.
 int tc_gemm_bf16(uint32_t M, uint32_t N, uint32_t K, const __nv_bfloat16* A, const __nv_bfloat16* W,

@@ -3,32 +3,35 @@
 // with new list N (nn ids) and old list O (no ids), the distance of every pair new[p] x new[p+1..]
 // and new[p] x old.  With R = N followed by O, all of them are entries above the diagonal of the
 // Gram matrix R[0:nn] R^T.  Several nodes share one MMA tile: their new rows first (the tile's
-// first rows, at most 128: the MMA's M side), then their old rows (at most 256 rows in all: N), so
+// first rows, at most 128: the MMA's M side), then their old rows (at most TR rows in all: N), so
 // that each node's Gram block sits on the diagonal of the tile's R_new R^T; K runs over 64-value
 // blocks of a BF16 copy of the base.
 //
-//   * CTAs are persistent and take 32 consecutive nodes at a time from a counter, packed in order
-//     into tiles.  Warps 0 and 2-9 gather a tile's rows with 16-byte cp.async copies (eight threads
-//     per 128-byte row segment) into a ring of stages in the 128-byte-swizzle K-major layout; each
-//     thread waits for its copies, fences them for the tensor cores (fence.proxy.async) and arrives
-//     on the stage's barrier.  The same stage is both MMA operands.  One thread of warp 1 issues the
-//     MMAs into TMEM.  Warps 2-9 copy the Gram rows of 32 new entries at a time out of TMEM (the two
-//     warps of each TMEM lane quarter taking alternate 32-column groups) into shared memory, then
-//     walk those entries' pairs in pair-array order, one pair per thread: distance
-//     ||x||^2 + ||y||^2 - 2 x.y, then the join's record step -- the same per-pair array, per-target
-//     counts and `found` flags as the FP32 join kernel.
-//   * Nodes too large for one tile (more than 128 new entries or 256 rows) are listed and scored by
-//     a second launch, tile by tile: a block of up to 128 new entries (the tile's first rows) with a
-//     chunk of the candidates after the block; the block's first chunk also covers the pairs within
-//     the block.  Each row's pairs in a tile are consecutive slots of the node's pair array.
+//   * Three launches per join.  Tiles of TR = 128 rows (128 TMEM columns: four CTAs per SM) take
+//     the nodes in order, 32 consecutive nodes at a time from a counter, packed in order; a node
+//     with more rows goes to a list that tiles of TR = 256 rows (two CTAs per SM) pack next; a node
+//     with more than 128 new entries or 256 rows goes to a second list, scored tile by tile: a
+//     block of new entries (the tile's first rows) with a chunk of the candidates after the block,
+//     the block's first chunk also covering the pairs within the block.  Each row's pairs in a
+//     tile are consecutive slots of its node's pair array.
+//   * CTAs are persistent.  Warps 0 and 2-9 gather a tile's rows with 16-byte cp.async copies
+//     (eight threads per 128-byte row segment) into a ring of stages in the 128-byte-swizzle
+//     K-major layout; each thread waits for its copies, fences them for the tensor cores
+//     (fence.proxy.async) and arrives on the stage's barrier.  The same stage is both MMA operands.
+//     One thread of warp 1 issues the MMAs into TMEM.  Warps 2-9 copy the Gram rows of 32 new
+//     entries at a time out of TMEM (the two warps of each TMEM lane quarter taking alternate
+//     32-column groups) into shared memory, then walk those entries' pairs in pair-array order, one
+//     pair per thread: distance ||x||^2 + ||y||^2 - 2 x.y, then the join's record step -- the same
+//     per-pair array, per-target counts and `found` flags as the FP32 join kernel.
 //   * When BF16 holds every value of the base, one product per value; with integer values and
 //     squared norms below 2^23 (byte data up to 128 dimensions) every sum is exact, so the distances
 //     equal the FP32 join's and the graph is identical.  Other data take the hi + lo split
 //     (hi.hi + hi.lo + lo.hi, a relative error near 2^-17 of sum |x_k y_k|): distances, and so pools,
 //     can then differ from the FP32 join's in the last bits.
-//   * Shared memory is sized so that at most two CTAs share an SM (two 256-column accumulators):
-//     a persistent CTA must never wait in tcgen05.alloc for columns another one holds.  Every wait is
-//     bounded; one that runs out sets the error word and the CTA leaves after its copies and MMAs.
+//   * Shared memory is sized so that the CTAs an SM can hold never need more than its 512 TMEM
+//     columns: a persistent CTA must never wait in tcgen05.alloc for columns another one holds.
+//     Every wait is bounded; one that runs out sets the error word and the CTA leaves after its
+//     copies and MMAs.
 #include <algorithm>
 
 #include "join.cuh"
@@ -39,17 +42,21 @@ namespace {
 
 using namespace tc;
 
-constexpr uint32_t JM = 128;          // new entries per node (MMA M, TMEM lanes)
-constexpr uint32_t JR = 256;          // rows per node (MMA N, TMEM columns)
+constexpr uint32_t JM = 128;          // new entries per tile (MMA M, TMEM lanes)
 constexpr uint32_t JKB = 64;          // BF16 values per k-block
-constexpr uint32_t JPART = JR * 128;  // one k-block of JR rows (32 KiB)
 constexpr uint32_t JREC = 8;          // record warps
 constexpr uint32_t JRT = JREC * 32;   // record threads
 constexpr uint32_t JTHREADS = 64 + JRT;
 constexpr uint32_t JPROD = JTHREADS - 32;  // row-gathering threads (every warp but the MMA warp)
-constexpr uint32_t DLD = JR + 1;      // row stride of the Gram rows in shared memory (conflict-free)
-constexpr uint32_t JCH = 32;          // consecutive nodes taken from the counter at a time
+constexpr uint32_t JCH = 32;          // nodes taken from the counter at a time
 constexpr uint32_t NONE = 0xffffffffu;
+
+// What a launch works on.
+enum : uint32_t {
+  MODE_ORDER = 0,  // every node in order, TR = 128: larger nodes go to the lists
+  MODE_LIST = 1,   // the nodes of list `mid` (<= 128 new entries, <= 256 rows), TR = 256
+  MODE_BIG = 2,    // the nodes of list `big`, tile by tile, TR = 256
+};
 
 struct JoinArgs {
   const __nv_bfloat16 *hi, *lo;  // BF16 rows of W values (lo only read when terms = 3)
@@ -60,12 +67,12 @@ struct JoinArgs {
   float* pairdist;
   uint32_t* cnt;
   uint8_t* found;
-  uint32_t* next_node;  // node counter (chunks of JCH nodes)
-  uint32_t* big;        // nodes larger than one tile: big[0] their count, then their ids
+  uint32_t* next_node;  // node counter of the launch
+  uint32_t* mid;        // nodes of 129 to 256 rows: mid[0] their count, then their ids
+  uint32_t* big;        // nodes larger than a tile: big[0] their count, then their ids
   int* err;
   uint64_t n;
-  uint32_t W, cap, P, check_k, kblocks, terms, nstages, stage_bytes;
-  uint32_t big_mode;  // 1: the listed nodes, each as tiles of up to 128 new rows x a chunk of candidates
+  uint32_t W, cap, P, check_k, kblocks, terms, nstages, mode;
 };
 
 // Offset of new entry p's first pair within the node's pairs (nn new, no old entries).
@@ -79,28 +86,42 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 
-__global__ void __launch_bounds__(JTHREADS, 2)
-    tc_join_kernel(const JoinArgs a) {
+template <uint32_t TR>
+struct Tile {
+  static constexpr uint32_t PART = TR * 128;  // one k-block of TR rows
+  static constexpr uint32_t DLD = TR + 1;     // row stride of the Gram rows in shared memory
+  static constexpr uint32_t BLOCK = TR / 2;   // new entries per block of a node larger than a tile
+  static size_t smem(uint32_t terms) {
+    const uint32_t nstages = terms == 1 ? 2 : 1;
+    return 1024 + (size_t)nstages * (terms == 1 ? 1 : 2) * PART + 32 * DLD * 4;
+  }
+};
+
+template <uint32_t TR>
+__global__ void __launch_bounds__(JTHREADS, 512 / TR) tc_join_kernel(const JoinArgs a) {
+  using TL = Tile<TR>;
+  constexpr uint32_t PART = TL::PART, DLD = TL::DLD;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_mma, bar_drain;
   __shared__ uint64_t po_ch[JCH];                  // pair-array offset of each node of the chunk
   __shared__ uint64_t rstart[JM];                  // slot of each tile new entry's first pair
-  __shared__ uint32_t nn_ch[JCH], no_ch[JCH];      // list lengths (nn 0: no pairs here)
+  __shared__ uint32_t id_ch[JCH], nn_ch[JCH], no_ch[JCH];  // the chunk's nodes (nn 0: no pairs here)
   __shared__ uint32_t tslot[JCH], tnb[JCH], tob[JCH];  // tile nodes: chunk slot, first new row, first old row
   __shared__ uint32_t cum[JM + 1];                 // pairs of the tile's new entries before each one
   __shared__ uint8_t rnode[JM];                    // tile node of each new entry
-  __shared__ uint32_t rows_sh[JR];                 // the tile's rows: all new entries, then all old ones
-  __shared__ float norm_sh[JR];
-  __shared__ uint32_t tmem_base_sh, i0_sh, chn_sh, chpos_sh, tn_sh, nsum_sh, tsum_sh;
+  __shared__ uint32_t rows_sh[TR];                 // the tile's rows: all new entries, then all old ones
+  __shared__ float norm_sh[TR];
+  __shared__ uint32_t tmem_base_sh, chn_sh, chpos_sh, tn_sh, nsum_sh, tsum_sh;
   __shared__ int abort_sh, rec_fail_sh, bad_sh;
-  // big mode: the node (its id, list lengths, pair offset), the next tile's new block and candidate
-  // chunk start, whether it is the block's first (the one with the triangle), and the tile taken
+  // MODE_BIG: the node (id, list lengths, pair offset), the next tile's block of new entries and
+  // candidate chunk start, whether it is the block's first (the one with the triangle), the tile
   __shared__ uint32_t bm_node, bm_nn, bm_no, bm_a0, bm_c0, bm_first, bm_tri, bm_tc0, bm_ch;
   __shared__ uint64_t bm_po;
   const uint32_t raw = smem_addr(smem_raw);
   const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
   const uint32_t sbase = raw + pad;
-  float* gram = reinterpret_cast<float*>(smem_raw + pad + a.nstages * a.stage_bytes);  // 32 x DLD
+  const uint32_t stage_bytes = (a.terms == 1 ? 1u : 2u) * PART;
+  float* gram = reinterpret_cast<float*>(smem_raw + pad + a.nstages * stage_bytes);  // 32 x DLD
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -118,7 +139,7 @@ __global__ void __launch_bounds__(JTHREADS, 2)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_sh)),
-                 "r"(JR)
+                 "r"(TR)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -133,8 +154,8 @@ __global__ void __launch_bounds__(JTHREADS, 2)
 
   for (;;) {
     __syncthreads();  // the previous tile's rows and entry arrays are no longer read
-    if (a.big_mode) {
-      // ---------------------------------------------------------- big mode: the next tile of a listed node
+    if (a.mode == MODE_BIG) {
+      // ---------------------------------------------------------- the next tile of a listed node
       if (threadIdx.x == 0) {
         uint32_t tn = 0;
         bad_sh = 0;
@@ -149,12 +170,12 @@ __global__ void __launch_bounds__(JTHREADS, 2)
             bm_no = a.old_cnt[i];
             bm_po = a.pair_off[i];
             bm_a0 = 0;
-            bm_c0 = min(JM, bm_nn);
+            bm_c0 = min(TL::BLOCK, bm_nn);
             bm_first = 1;
           }
-          const uint32_t nn = bm_nn, T = nn + bm_no, A = min(JM, nn - bm_a0);
+          const uint32_t nn = bm_nn, T = nn + bm_no, A = min(TL::BLOCK, nn - bm_a0);
           if (bm_c0 < T || (bm_first && A > 1)) {  // a tile with pairs
-            const uint32_t ch = min(JR - A, T - bm_c0);
+            const uint32_t ch = min(TR - A, T - bm_c0);
             bm_tri = bm_first;
             bm_tc0 = bm_c0;
             bm_ch = ch;
@@ -168,7 +189,7 @@ __global__ void __launch_bounds__(JTHREADS, 2)
           bm_a0 += A;  // the next block of new entries, or the next node
           if (bm_a0 >= nn) bm_node = NONE;
           else {
-            bm_c0 = min(bm_a0 + JM, nn);
+            bm_c0 = min(bm_a0 + TL::BLOCK, nn);
             bm_first = 1;
           }
         }
@@ -181,7 +202,7 @@ __global__ void __launch_bounds__(JTHREADS, 2)
       for (uint32_t b = threadIdx.x; b < tsum_sh; b += JTHREADS) {
         const uint32_t c = b < A ? a0 + b : c0 + (b - A);  // entry of the node's lists (new, then old)
         uint32_t r = c < nn ? a.new_ids[i * a.cap + c] : a.old_ids[i * a.cap + c - nn];
-        if (r >= a.n) {
+        if (r >= a.n) {  // not a row: reported, the tile left out
           bad_sh = 1;
           r = 0;
         }
@@ -194,87 +215,90 @@ __global__ void __launch_bounds__(JTHREADS, 2)
         }
       }
     } else {
-    if (chpos_sh >= chn_sh) {  // the chunk is packed: the next JCH nodes
-      if (threadIdx.x == 0) i0_sh = *abort_flag ? (uint32_t)a.n : atomicAdd(a.next_node, JCH);
-      __syncthreads();
-      const uint64_t i0 = i0_sh;
-      if (i0 >= a.n) break;
-      const uint32_t cn = a.n - i0 < JCH ? (uint32_t)(a.n - i0) : JCH;
-      if (threadIdx.x < cn) {
-        const uint64_t i = i0 + threadIdx.x;
-        uint32_t nn = a.new_cnt[i];
-        const uint32_t no = a.old_cnt[i];
-        if (nn > a.cap || no > a.cap) {  // not a list: reported, the node left out
-          atomicOr(a.err, 4);
-          nn = 0;
-        } else if (nn > 0 && (nn > JM || nn + no > JR)) {  // too large for one tile
-          a.big[1 + atomicAdd(a.big, 1u)] = (uint32_t)i;
-          nn = 0;
+      // ---------------------------------------------------------- packed tiles
+      if (chpos_sh >= chn_sh) {  // the chunk is packed: the next JCH nodes
+        if (threadIdx.x == 0) {
+          const uint32_t total = a.mode == MODE_LIST ? a.mid[0] : (uint32_t)a.n;
+          const uint32_t k0 = *abort_flag ? total : atomicAdd(a.next_node, JCH);
+          chn_sh = k0 < total ? min(JCH, total - k0) : 0;
+          chpos_sh = k0;  // (the chunk's first position, for the loads below)
         }
-        nn_ch[threadIdx.x] = nn;
-        no_ch[threadIdx.x] = no;
-        po_ch[threadIdx.x] = a.pair_off[i];
+        __syncthreads();
+        const uint32_t cn = chn_sh;
+        if (cn == 0) break;
+        if (threadIdx.x < cn) {
+          const uint32_t k = chpos_sh + threadIdx.x;
+          const uint32_t i = a.mode == MODE_LIST ? a.mid[1 + k] : k;
+          uint32_t nn = a.new_cnt[i];
+          const uint32_t no = a.old_cnt[i];
+          if (nn > a.cap || no > a.cap) {  // not a list: reported, the node left out
+            atomicOr(a.err, 4);
+            nn = 0;
+          } else if (nn > 0 && a.mode == MODE_ORDER && (nn > JM || nn + no > TR)) {
+            if (nn <= JM && nn + no <= 256) a.mid[1 + atomicAdd(a.mid, 1u)] = i;  // for TR = 256
+            else a.big[1 + atomicAdd(a.big, 1u)] = i;                                // tile by tile
+            nn = 0;
+          }
+          id_ch[threadIdx.x] = i;
+          nn_ch[threadIdx.x] = nn;
+          no_ch[threadIdx.x] = no;
+          po_ch[threadIdx.x] = a.pair_off[i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) chpos_sh = 0;
       }
-      if (threadIdx.x == 0) {
-        chn_sh = cn;
-        chpos_sh = 0;
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {  // the next nodes of the chunk that fit one tile together
-      const uint32_t cn = chn_sh;
-      uint32_t pos = chpos_sh, tn = 0, ns = 0, ts = 0;
-      if (*abort_flag) pos = cn;
-      while (pos < cn) {
-        const uint32_t nn = nn_ch[pos], t = nn + no_ch[pos];
-        if (nn == 0) {
+      if (threadIdx.x == 0) {  // the next nodes of the chunk that fit one tile together
+        const uint32_t cn = chn_sh;
+        uint32_t pos = chpos_sh, tn = 0, ns = 0, ts = 0;
+        if (*abort_flag) pos = cn;
+        while (pos < cn) {
+          const uint32_t nn = nn_ch[pos], t = nn + no_ch[pos];
+          if (nn == 0) {
+            ++pos;
+            continue;
+          }
+          if (ns + nn > JM || ts + t > TR) break;
+          tslot[tn] = pos;
+          tnb[tn] = ns;
+          ns += nn;
+          ts += t;
+          ++tn;
           ++pos;
-          continue;
         }
-        if (ns + nn > JM || ts + t > JR) break;
-        tslot[tn] = pos;
-        tnb[tn] = ns;
-        ns += nn;
-        ts += t;
-        ++tn;
-        ++pos;
-      }
-      for (uint32_t j = 0, o = ns; j < tn; ++j) {
-        tob[j] = o;
-        o += no_ch[tslot[j]];
-      }
-      chpos_sh = pos;
-      tn_sh = tn;
-      nsum_sh = ns;
-      tsum_sh = ts;
-      bad_sh = 0;
-      rec_fail_sh = 0;
-    }
-    __syncthreads();
-    if (tn_sh == 0) continue;
-    const uint64_t i0 = i0_sh;
-    for (uint32_t j = warp; j < tn_sh; j += JTHREADS / 32) {  // a warp per tile node
-      const uint32_t sl = tslot[j], nn = nn_ch[sl], no = no_ch[sl];
-      const uint64_t i = i0 + sl;
-      for (uint32_t e = lane; e < nn + no; e += 32) {
-        uint32_t r = e < nn ? a.new_ids[i * a.cap + e] : a.old_ids[i * a.cap + e - nn];
-        if (r >= a.n) {  // not a row: reported, the tile left out
-          bad_sh = 1;
-          r = 0;
+        for (uint32_t j = 0, o = ns; j < tn; ++j) {
+          tob[j] = o;
+          o += no_ch[tslot[j]];
         }
-        const uint32_t b = e < nn ? tnb[j] + e : tob[j] + e - nn;
-        rows_sh[b] = r;
-        norm_sh[b] = a.xnorm[r];
-        if (e < nn) {
-          rnode[b] = (uint8_t)j;
-          rstart[b] = po_ch[sl] + pair_row(nn, no, e);
+        chpos_sh = pos;
+        tn_sh = tn;
+        nsum_sh = ns;
+        tsum_sh = ts;
+        bad_sh = 0;
+        rec_fail_sh = 0;
+      }
+      __syncthreads();
+      if (tn_sh == 0) continue;
+      for (uint32_t j = warp; j < tn_sh; j += JTHREADS / 32) {  // a warp per tile node
+        const uint32_t sl = tslot[j], nn = nn_ch[sl], no = no_ch[sl];
+        const uint64_t i = id_ch[sl];
+        for (uint32_t e = lane; e < nn + no; e += 32) {
+          uint32_t r = e < nn ? a.new_ids[i * a.cap + e] : a.old_ids[i * a.cap + e - nn];
+          if (r >= a.n) {  // not a row: reported, the tile left out
+            bad_sh = 1;
+            r = 0;
+          }
+          const uint32_t b = e < nn ? tnb[j] + e : tob[j] + e - nn;
+          rows_sh[b] = r;
+          norm_sh[b] = a.xnorm[r];
+          if (e < nn) {
+            rnode[b] = (uint8_t)j;
+            rstart[b] = po_ch[sl] + pair_row(nn, no, e);
+          }
         }
       }
-    }
     }
     __syncthreads();
     const uint32_t Ns = nsum_sh, Ts = tsum_sh, Tpad = (Ts + 15) & ~15u;
-    const uint64_t i0 = i0_sh;  // (packed tiles) the chunk's first node
     if (bad_sh) {
       if (threadIdx.x == 0) atomicOr(a.err, 4);
       continue;
@@ -292,13 +316,13 @@ __global__ void __launch_bounds__(JTHREADS, 2)
           ok = false;
           break;
         }
-        const uint32_t st = sbase + s * a.stage_bytes;
+        const uint32_t st = sbase + s * stage_bytes;
         for (uint32_t e = pt; e < Ts * 8; e += JPROD) {
           const uint32_t r = e >> 3, j = e & 7;
           const uint64_t off = (uint64_t)rows_sh[r] * a.W + kb * JKB + j * 8;
           const uint32_t dst = st + r * 128 + ((j ^ (r & 7)) << 4);
           cp_async16(dst, a.hi + off);
-          if (a.terms != 1) cp_async16(dst + JPART, a.lo + off);
+          if (a.terms != 1) cp_async16(dst + PART, a.lo + off);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
         if (a.nstages > 1 && kb > 0) {  // the previous k-block's copies are done: hand its stage over
@@ -331,8 +355,8 @@ __global__ void __launch_bounds__(JTHREADS, 2)
             break;
           }
           tc_fence_after();
-          const uint32_t st = sbase + s * a.stage_bytes;
-          const uint64_t dh = sw128_desc(st), dl = sw128_desc(st + JPART);
+          const uint32_t st = sbase + s * stage_bytes;
+          const uint64_t dh = sw128_desc(st), dl = sw128_desc(st + PART);
 #pragma unroll
           for (uint32_t j = 0; j < JKB / 16; ++j) {
             const uint64_t o = (uint64_t)(2 * j);
@@ -351,13 +375,14 @@ __global__ void __launch_bounds__(JTHREADS, 2)
     } else if (warp >= 2) {
       // ------------------------------------------------------------ records (warps 2-9)
       const uint32_t t = threadIdx.x - 64, quad = warp & 3u, half = (warp - 2) >> 2;
+      const bool big = a.mode == MODE_BIG;
       if (warp == 2) {  // cum: prefix sums of the new entries' pair counts
         uint32_t carry = 0;
         for (uint32_t r0 = 0; r0 < Ns; r0 += 32) {
           const uint32_t r = r0 + lane;
           uint32_t v = 0;
           if (r < Ns) {
-            if (a.big_mode) {
+            if (big) {
               v = (bm_tri ? Ns - r - 1 : 0) + bm_ch;
             } else {
               const uint32_t j = rnode[r], sl = tslot[j];
@@ -400,10 +425,10 @@ __global__ void __launch_bounds__(JTHREADS, 2)
           for (uint32_t u = cum[q0] + t; u < u1; u += JRT) {
             while (u >= cum[r + 1]) ++r;
             const uint32_t off = u - cum[r];
-            uint32_t bc;     // the candidate's row in the tile
-            bool cand_new;   // the candidate is a new entry
+            uint32_t bc;    // the candidate's row in the tile
+            bool cand_new;  // the candidate is a new entry
             uint64_t node;
-            if (a.big_mode) {
+            if (big) {
               const uint32_t tl = bm_tri ? Ns - r - 1 : 0;  // the row's pairs within the new block
               if (off < tl) {
                 bc = r + 1 + off;
@@ -418,7 +443,7 @@ __global__ void __launch_bounds__(JTHREADS, 2)
               const uint32_t cl = r - tnb[j] + 1 + off;  // candidate within the node's lists
               bc = cl < nn ? tnb[j] + cl : tob[j] + (cl - nn);
               cand_new = cl < nn;
-              node = i0 + sl;
+              node = id_ch[sl];
             }
             const float dot = gram[(r - q0) * DLD + bc];
             const float d = fmaxf(fmaf(-2.f, dot, norm_sh[r] + norm_sh[bc]), 0.f);
@@ -451,13 +476,34 @@ __global__ void __launch_bounds__(JTHREADS, 2)
     }
     __syncwarp();
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(JR) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TR) : "memory");
   }
 }
 
-size_t join_smem(uint32_t terms) {
-  const uint32_t nstages = terms == 1 ? 2 : 1;
-  return 1024 + (size_t)nstages * (terms == 1 ? 1 : 2) * JPART + 32 * DLD * 4;
+// One launch of tc_join_kernel<TR>: persistent CTAs, as many per SM as TMEM allows (512 / TR).
+template <uint32_t TR>
+int launch_join(const JoinArgs& a, int sms, int smem_max, cudaStream_t s) {
+  // shared memory keeps the CTAs of an SM within its 512 TMEM columns: more than 512 / TR of them
+  // must not fit
+  size_t smem = Tile<TR>::smem(a.terms);
+  int dev = 0, sm_smem = 0, reserved = 0;
+  EFG_CUDA(cudaGetDevice(&dev));
+  EFG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  EFG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+  cudaFuncAttributes fa;
+  EFG_CUDA(cudaFuncGetAttributes(&fa, tc_join_kernel<TR>));
+  const size_t fixed = fa.sharedSizeBytes + (size_t)reserved;
+  const size_t floor_per_cta = (size_t)sm_smem / (512 / TR + 1) + 1;  // more than 512 / TR do not fit
+  if (smem + fixed < floor_per_cta) smem = floor_per_cta - fixed;
+  if ((int64_t)smem > smem_max) return fail(EFG_ERR_ARG, "tensor-core join: shared memory");
+  EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel<TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel<TR>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared));
+  // (the occupancy calculator can answer fewer CTAs than fit; the CTAs are persistent, so one that
+  // does not fit beside the others starts after them and finds the node counter spent)
+  tc_join_kernel<TR><<<(unsigned)(sms * (512 / TR)), JTHREADS, smem, s>>>(a);
+  EFG_CUDA(cudaGetLastError());
+  return EFG_OK;
 }
 
 }  // namespace
@@ -477,17 +523,17 @@ int tc_join_prepare(const float* base, uint64_t n, uint32_t dim, uint32_t ld, __
   return EFG_OK;
 }
 
-// Join pass 0 on the tensor cores.  big_mode 0: every node that fits one tile, packed several to a
-// tile; the others are listed in big (big[0] their count, then their ids), which must be zero on
-// entry.  big_mode 1: the listed nodes, each as tiles of up to 128 new entries x up to 256 rows.
-// next_node (a node counter of each launch) and *err must be zero on entry.  terms: 1 (BF16 holds
-// the base) or 3 (hi + lo products).
+// Join pass 0 on the tensor cores: three launches (tiles of 128 rows over every node, tiles of 256
+// rows over the nodes listed in mid, and the nodes listed in big tile by tile).  counters: three
+// node counters, zero on entry; mid and big: n + 1 words each, their counts (word 0) zero on entry;
+// *err zero on entry.  terms: 1 (BF16 holds the base) or 3 (hi + lo products).
 int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms, uint64_t n, uint32_t dim,
             uint32_t terms, uint32_t cap, uint32_t P, uint32_t check_k, const uint32_t* new_ids,
             const uint32_t* new_cnt, const uint32_t* old_ids, const uint32_t* old_cnt, const uint64_t* pair_off,
-            const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* next_node, uint32_t* big,
-            int big_mode, int* err, cudaStream_t s) {
+            const float* bound, float* pairdist, uint32_t* cnt, uint8_t* found, uint32_t* counters, uint32_t* mid,
+            uint32_t* big, int* err, cudaStream_t s) {
   if (terms != 1 && terms != 3) return fail(EFG_ERR_ARG, "tensor-core join: terms must be 1 or 3");
+  if (n >= 0xffffffffull) return fail(EFG_ERR_ARG, "tensor-core join: more than 2^32 - 2 rows");
   const uint32_t W = (dim + 63) / 64 * 64;
   int dev = 0, sms = 148, smem_max = 0;
   EFG_CUDA(cudaGetDevice(&dev));
@@ -506,7 +552,7 @@ int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms
   a.pairdist = pairdist;
   a.cnt = cnt;
   a.found = found;
-  a.next_node = next_node;
+  a.mid = mid;
   a.big = big;
   a.err = err;
   a.n = n;
@@ -517,20 +563,15 @@ int tc_join(const __nv_bfloat16* hi, const __nv_bfloat16* lo, const float* norms
   a.kblocks = W / JKB;
   a.terms = terms;
   a.nstages = terms == 1 ? 2 : 1;
-  a.stage_bytes = (terms == 1 ? 1u : 2u) * JPART;
-  a.big_mode = big_mode ? 1u : 0u;
-  // about 97 KB per CTA: two fit on an SM, three do not (two 256-column accumulators fill TMEM)
-  const size_t smem = join_smem(terms);
-  if ((int64_t)smem > smem_max) return fail(EFG_ERR_ARG, "tensor-core join: shared memory");
-  EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // the whole shared-memory carveout, so that two CTAs fit an SM
-  EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                (int)cudaSharedmemCarveoutMaxShared));
-  // two CTAs per SM (the occupancy calculator can answer one where two fit); the CTAs are
-  // persistent, so a second one that does not fit next to the first starts after it and finds the
-  // node counter spent
-  tc_join_kernel<<<(unsigned)(sms * 2), JTHREADS, smem, s>>>(a);
-  EFG_CUDA(cudaGetLastError());
+  a.mode = MODE_ORDER;
+  a.next_node = counters;
+  EFG_TRY(launch_join<128>(a, sms, smem_max, s));
+  a.mode = MODE_LIST;
+  a.next_node = counters + 1;
+  EFG_TRY(launch_join<256>(a, sms, smem_max, s));
+  a.mode = MODE_BIG;
+  a.next_node = counters + 2;
+  EFG_TRY(launch_join<256>(a, sms, smem_max, s));
   return EFG_OK;
 }
 

@@ -51,7 +51,7 @@ struct NNDev {
   DevBuf<__nv_bfloat16> jhi, jlo;
   DevBuf<float> jnorm;
   DevBuf<int> jflag;
-  DevBuf<uint32_t> jbig;
+  DevBuf<uint32_t> jmid, jbig;  // nodes of 129-256 rows, and larger ones (count in word 0)
   uint32_t jterms = 0;  // 0: not prepared; 1 or 3 products per value
   void release_all() {
     pd.release(); radius.release(); radiusM.release(); pid.release(); Lc.release(); Range.release();
@@ -59,6 +59,7 @@ struct NNDev {
     pair_off.release(); rec_off64.release(); scan64.release(); pairdist.release(); cnt.release(); cursor.release();
     rec_aux.release(); rcnt.release(); rcur.release(); roff.release(); rbuf.release(); scan32.release();
     ucnt.release(); rec_key.release(); jhi.release(); jlo.release(); jnorm.release(); jflag.release();
+    jmid.release();
     jbig.release();
     jterms = 0;
   }
@@ -612,18 +613,18 @@ __device__ __forceinline__ uint32_t warp_argmin(K96 x) {
 // One warp per target node: applies its records in ascending (dist, id, source, side) order,
 // every one of them (repeats of a record included), with Neighbor::insert / InsertIntoKnn
 // semantics (base_index.hpp:37-61).  The order comes from one of three sources:
-//   * up to msort records: sorted once in the warp's shared memory;
+//   * 129 to msort records: sorted once in the warp's shared memory;
 //   * up to 32 x msort: runs of msort sorted in shared memory and written back in place, then
-//     merged 32 ways (lane l holds run l's head; 32 records of each run staged in shared memory);
-//   * more: pulled 32 at a time by scanning all of them.
+//     merged 32 ways (lane l holds run l's head; msort / 32 records of each run staged in shared
+//     memory);
+//   * up to 128, or more than 32 x msort: pulled 32 at a time by scanning all of them.
 // The reference rejects a candidate whose id sits among the entries of equal distance; a pair's
 // distance is the same wherever the reference computes it, so that finds every repeat.  With
 // any_dist a repeat is found at any distance: the tensor-core join's distances can differ in the
 // last bits from the FP32 ones a pool entry was inserted with, and an equal-distance test would
 // let the id in twice.
 template <int NS>
-__global__ void __launch_bounds__(MERGE_WARPS * 32)
-    merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_dist, uint32_t msort,
+__global__ void merge_kernel(uint64_t n, uint32_t P, uint32_t check_k, bool any_dist, uint32_t msort,
                  const uint32_t* __restrict__ cnt, const uint64_t* __restrict__ rec_off, uint64_t* __restrict__ rec_key,
                  uint32_t* __restrict__ rec_aux, float* __restrict__ pd, uint32_t* __restrict__ pid,
                  uint32_t* __restrict__ Lc, float* __restrict__ radius, uint8_t* __restrict__ found,
@@ -721,7 +722,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32)
   };
 
   const uint32_t runs = (B + msort - 1) / msort;
-  if (runs <= 32) {
+  if (B > 128 && runs <= 32) {  // (a few batches of a small node: scanning, which stops at a rejection)
     // sort each run of msort records in shared memory (a single run stays there)
     for (uint32_t q = 0; q < runs; ++q) {
       const uint32_t b0 = q * msort, len = min(msort, B - b0);
@@ -1126,9 +1127,9 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   EFG_CUDA(cudaMemsetAsync(S.cnt.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.cursor.p, 0, n * 4, s));
   EFG_CUDA(cudaMemsetAsync(S.found.p, 0, n, s));
-  LocalBuf<uint32_t> jctr;  // node counters of the two join passes, the merge and the FP32 node list
-  EFG_TRY(jctr.reserve(4));
-  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 16, s));
+  LocalBuf<uint32_t> jctr;  // node counters of the two join passes, the merge, the tensor-core join's three
+  EFG_TRY(jctr.reserve(6));
+  EFG_CUDA(cudaMemsetAsync(jctr.p, 0, 24, s));
   int sms = 152, per0 = 1, per1 = 1, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1145,6 +1146,7 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
       EFG_TRY(S.jlo.reserve(n * W));
       EFG_TRY(S.jnorm.reserve(n));
       EFG_TRY(S.jflag.reserve(2));
+      EFG_TRY(S.jmid.reserve(n + 1));
       EFG_TRY(S.jbig.reserve(n + 1));
       EFG_TRY(tc_join_prepare(idx->d_base, n, idx->dim, idx->ld, S.jhi.p, S.jlo.p, S.jnorm.p, S.jflag.p, s));
       int inexact = 0;
@@ -1153,11 +1155,11 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
       S.jterms = inexact ? 3 : 1;
     }
     EFG_CUDA(cudaMemsetAsync(S.jflag.p + 1, 0, 4, s));
+    EFG_CUDA(cudaMemsetAsync(S.jmid.p, 0, 4, s));
     EFG_CUDA(cudaMemsetAsync(S.jbig.p, 0, 4, s));
-    for (int big_mode = 0; big_mode < 2; ++big_mode)  // the nodes of one tile, then the larger ones
-      EFG_TRY(tc_join(S.jhi.p, S.jlo.p, S.jnorm.p, n, idx->dim, S.jterms, S.cap, S.P, bp.check_k, S.new_ids.p,
-                      S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
-                      S.found.p, big_mode ? jctr.p + 3 : jctr.p, S.jbig.p, big_mode, S.jflag.p + 1, s));
+    EFG_TRY(tc_join(S.jhi.p, S.jlo.p, S.jnorm.p, n, idx->dim, S.jterms, S.cap, S.P, bp.check_k, S.new_ids.p,
+                    S.new_cnt.p, S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p, S.found.p,
+                    jctr.p + 3, S.jmid.p, S.jbig.p, S.jflag.p + 1, s));
   } else {
     join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
                                             S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,

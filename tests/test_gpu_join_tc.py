@@ -36,6 +36,7 @@ STATE_CASES = [
     (3000, 32, dict(trees=8, merge_level=4, epochs=4, check=25, L=30, K=10, S=10)),
     (2500, 128, dict(trees=4, merge_level=3, epochs=3, check=40, L=20, K=8, S=6)),
     (2000, 64, dict(trees=6, merge_level=4, epochs=3, check=60, L=50, K=20, S=12)),
+    (1500, 96, dict(trees=4, merge_level=3, epochs=3, check=150, L=150, K=20, S=10)),
 ]
 
 

@@ -183,6 +183,9 @@ NND_CASES = [
     (2500, 48, dict(trees=4, merge_level=3, epochs=4, check=40, L=20, K=8, S=6)),
     (2000, 16, dict(trees=6, merge_level=4, epochs=4, check=60, L=50, K=20, S=12)),
     (2000, 24, dict(trees=4, merge_level=3, epochs=3, check=10, L=12, K=5, S=4)),
+    # pools of 101 and 151 entries: the merge's four- and eight-slot warp pools
+    (2000, 16, dict(trees=4, merge_level=3, epochs=3, check=100, L=100, K=20, S=10)),
+    (1500, 24, dict(trees=4, merge_level=3, epochs=3, check=150, L=150, K=20, S=10)),
 ]
 
 

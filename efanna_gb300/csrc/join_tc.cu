@@ -7,7 +7,7 @@
 // that each node's Gram block sits on the diagonal of the tile's R_new R^T; K runs over 64-value
 // blocks of a BF16 copy of the base.
 //
-//   * Three launches per join.  Tiles of TR = 128 rows (128 TMEM columns: four CTAs per SM) take
+//   * Three launches per join.  Tiles of TR = 128 rows (128 TMEM columns, three CTAs per SM) take
 //     the nodes in order, 32 consecutive nodes at a time from a counter, packed in order; a node
 //     with more rows goes to a list that tiles of TR = 256 rows (two CTAs per SM) pack next; a node
 //     with more than 128 new entries or 256 rows goes to a second list, scored tile by tile: a
@@ -88,6 +88,9 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
 
 template <uint32_t TR>
 struct Tile {
+  // CTAs per SM: three 128-column accumulators (a quarter of TMEM left free: four CTAs of 128 rows,
+  // all 512 columns, stalled large builds), two of 256
+  static constexpr uint32_t CTAS = TR == 128 ? 3 : 2;
   static constexpr uint32_t PART = TR * 128;  // one k-block of TR rows
   static constexpr uint32_t DLD = TR + 1;     // row stride of the Gram rows in shared memory
   static constexpr uint32_t BLOCK = TR / 2;   // new entries per block of a node larger than a tile
@@ -98,7 +101,7 @@ struct Tile {
 };
 
 template <uint32_t TR>
-__global__ void __launch_bounds__(JTHREADS, 512 / TR) tc_join_kernel(const JoinArgs a) {
+__global__ void __launch_bounds__(JTHREADS, Tile<TR>::CTAS) tc_join_kernel(const JoinArgs a) {
   using TL = Tile<TR>;
   constexpr uint32_t PART = TL::PART, DLD = TL::DLD;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -480,11 +483,11 @@ __global__ void __launch_bounds__(JTHREADS, 512 / TR) tc_join_kernel(const JoinA
   }
 }
 
-// One launch of tc_join_kernel<TR>: persistent CTAs, as many per SM as TMEM allows (512 / TR).
+// One launch of tc_join_kernel<TR>: persistent CTAs, Tile<TR>::CTAS per SM.
 template <uint32_t TR>
 int launch_join(const JoinArgs& a, int sms, int smem_max, cudaStream_t s) {
-  // shared memory keeps the CTAs of an SM within its 512 TMEM columns: more than 512 / TR of them
-  // must not fit
+  // shared memory keeps the CTAs of an SM within its TMEM columns: more than CTAS of them must not
+  // fit
   size_t smem = Tile<TR>::smem(a.terms);
   int dev = 0, sm_smem = 0, reserved = 0;
   EFG_CUDA(cudaGetDevice(&dev));
@@ -493,7 +496,7 @@ int launch_join(const JoinArgs& a, int sms, int smem_max, cudaStream_t s) {
   cudaFuncAttributes fa;
   EFG_CUDA(cudaFuncGetAttributes(&fa, tc_join_kernel<TR>));
   const size_t fixed = fa.sharedSizeBytes + (size_t)reserved;
-  const size_t floor_per_cta = (size_t)sm_smem / (512 / TR + 1) + 1;  // more than 512 / TR do not fit
+  const size_t floor_per_cta = (size_t)sm_smem / (Tile<TR>::CTAS + 1) + 1;  // more than CTAS do not fit
   if (smem + fixed < floor_per_cta) smem = floor_per_cta - fixed;
   if ((int64_t)smem > smem_max) return fail(EFG_ERR_ARG, "tensor-core join: shared memory");
   EFG_CUDA(cudaFuncSetAttribute(tc_join_kernel<TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -501,7 +504,7 @@ int launch_join(const JoinArgs& a, int sms, int smem_max, cudaStream_t s) {
                                 (int)cudaSharedmemCarveoutMaxShared));
   // (the occupancy calculator can answer fewer CTAs than fit; the CTAs are persistent, so one that
   // does not fit beside the others starts after them and finds the node counter spent)
-  tc_join_kernel<TR><<<(unsigned)(sms * (512 / TR)), JTHREADS, smem, s>>>(a);
+  tc_join_kernel<TR><<<(unsigned)(sms * Tile<TR>::CTAS), JTHREADS, smem, s>>>(a);
   EFG_CUDA(cudaGetLastError());
   return EFG_OK;
 }

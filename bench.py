@@ -626,7 +626,7 @@ P960_LADDER = [(4, 1200, 200), (4, 2000, 300), (6, 3000, 300), (8, 4000, 300), (
 
 
 def measure_precision_960(E, args, hbm, peak_kind):
-    """BASELINE's high-dimensional precision workload: N x 960 vectors of the unit-block generator
+    """The high-dimensional precision workload: N x 960 vectors of the unit-block generator
     (values in [0, 1], L1-normalised blocks of 16; drawn on the GPU), a K = 100 graph (trees 8,
     ml 8, iter 8, L 200, check 200, S 10) searched with its own 8 trees; 10k held-out queries,
     k = 100.  Reports the build, recall@100 of FP32, BF16 and FP8 screening (FP32 re-rank) against
@@ -774,7 +774,7 @@ C5_REFERENCE = (8, 8000, 800)  # the plain search the traces' rungs are scored a
 
 
 def measure_learned_aniso(E, args, n=None, decay=0.35, plain_ladder=None, rungs=None, reference=None, ntrain=None):
-    """BASELINE's learned-form workload: N = 10M x 96 from the seeded anisotropic 1,024-component
+    """The learned-form workload: N = 10M x 96 from the seeded anisotropic 1,024-component
     mixture (drawn on the GPU), a K = 32 graph (trees 8, ml 8, iter 8, L 40, check 40, S 10) and 16
     search trees; 100k held-out test queries (recall judged on the first 2,000 by the exact
     10-NN), k = 10.  The plain BF16 search along a ladder of settings, then the learned form: k-means

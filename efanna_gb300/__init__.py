@@ -164,6 +164,9 @@ def lib():
         "efg_graph_size": (u64, [vp]),
         "efg_graph_row": (C.c_int64, [vp, u64, C.POINTER(C.c_uint32), u64]),
         "efg_graph_csr": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]),
+        "efg_graph_csc": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
+        "efg_csr_transpose": (i32, [u64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_uint32)]),
         "efg_tree_count": (u32, [vp]),
         "efg_last_error": (C.c_char_p, []),
         "efg_version": (C.c_char_p, []),
@@ -382,6 +385,18 @@ class Index:
         _check(lib().efg_graph_csr(self._h, ptr.ctypes.data_as(C.POINTER(C.c_uint64)),
                                    ids.ctypes.data_as(C.POINTER(C.c_uint32)), None))
         return ptr, ids[:nnz.value]
+
+    def graph_csc(self):
+        """The graph in compressed-column form (the MATLAB front end's getGraphMat): col_ptr (n + 1) and
+        row_ids, column j holding the nodes whose rows list j, ascending."""
+        n = self.graph_size()
+        nnz = C.c_uint64()
+        _check(lib().efg_graph_csr(self._h, None, None, C.byref(nnz)))
+        col_ptr = np.zeros(n + 1, np.uint64)
+        row_ids = np.zeros(max(1, nnz.value), np.uint32)
+        _check(lib().efg_graph_csc(self._h, col_ptr.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                   row_ids.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return col_ptr, row_ids[:nnz.value]
 
     def graph(self) -> np.ndarray:
         """Fixed-degree graph as an (n, K) array."""
@@ -650,6 +665,19 @@ def knn_stats() -> KnnStats:
     st = KnnStats()
     _check(lib().efg_get_knn_stats(C.byref(st)))
     return st
+
+
+def csr_transpose(row_ptr: np.ndarray, ids: np.ndarray, n: int):
+    """efg_csr_transpose: the compressed-column form of a CSR graph over n nodes (host arrays)."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.uint64)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    col_ptr = np.zeros(n + 1, np.uint64)
+    row_ids = np.zeros(max(1, int(row_ptr[n])), np.uint32)
+    _check(lib().efg_csr_transpose(n, row_ptr.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                   ids.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                   col_ptr.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                   row_ids.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return col_ptr, row_ids[:int(row_ptr[n])]
 
 
 def brute_force_knn_device(base_ptr: int, n: int, dim: int, row_stride: int, q_ptr: int, nq: int, q_stride: int,

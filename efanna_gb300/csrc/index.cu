@@ -651,6 +651,37 @@ int efg_graph_csr(const efg_index* idx, uint64_t* row_ptr, uint32_t* ids, uint64
   return EFG_OK;
 }
 
+int efg_csr_transpose(uint64_t n, const uint64_t* row_ptr, const uint32_t* ids, uint64_t* col_ptr,
+                      uint32_t* row_ids) {
+  if (!row_ptr || !col_ptr || (!ids && row_ptr[n]) || (!row_ids && row_ptr[n])) return fail(EFG_ERR_ARG, "null argument");
+  if (row_ptr[0] != 0) return fail(EFG_ERR_ARG, "row_ptr[0] must be 0");
+  for (uint64_t i = 0; i < n; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return fail(EFG_ERR_ARG, "row_ptr must be ascending");
+  const uint64_t nnz = row_ptr[n];
+  // counting sort by column; sources visited in ascending order keep each column's rows ascending
+  std::vector<uint64_t> cnt(n + 1, 0);
+  for (uint64_t e = 0; e < nnz; ++e) {
+    if (ids[e] >= n) return fail(EFG_ERR_ARG, "graph id " + std::to_string(ids[e]) + " >= n");
+    ++cnt[ids[e] + 1];
+  }
+  for (uint64_t j = 0; j < n; ++j) cnt[j + 1] += cnt[j];
+  for (uint64_t j = 0; j <= n; ++j) col_ptr[j] = cnt[j];
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t e = row_ptr[i]; e < row_ptr[i + 1]; ++e) row_ids[cnt[ids[e]]++] = (uint32_t)i;
+  return EFG_OK;
+}
+
+int efg_graph_csc(const efg_index* idx, uint64_t* col_ptr, uint32_t* row_ids) {
+  if (!idx || !col_ptr) return fail(EFG_ERR_ARG, "null argument");
+  if (!idx->graph.valid) return fail(EFG_ERR_STATE, "no graph");
+  const uint64_t n = idx->graph.n, nnz = idx->graph.nnz;
+  if (nnz && !row_ids) return fail(EFG_ERR_ARG, "null argument");
+  std::vector<uint64_t> ptr(n + 1);
+  std::vector<uint32_t> ids(nnz);
+  EFG_TRY(efg_graph_csr(idx, ptr.data(), ids.data(), nullptr));
+  return efg_csr_transpose(n, ptr.data(), ids.data(), col_ptr, row_ids);
+}
+
 uint32_t efg_tree_count(const efg_index* idx) { return idx ? idx->forest.ntrees : 0; }
 
 int efg_l2_pairs(const float* d_base, uint64_t n, uint32_t dim, uint64_t row_stride, const uint32_t* d_a,

@@ -329,6 +329,15 @@ uint64_t efg_graph_size(const efg_index* idx);
 int64_t efg_graph_row(const efg_index* idx, uint64_t row, uint32_t* out, uint64_t cap);
 /* Whole graph as CSR: row_ptr[n+1] and ids[nnz] (host buffers; pass NULL to query nnz). */
 int efg_graph_csr(const efg_index* idx, uint64_t* row_ptr, uint32_t* ids, uint64_t* nnz);
+/* The graph as the MATLAB front end's sparse matrix (findex.cc:106-150, getGraphMat): entry (i, j)
+ * for every neighbour j of node i, in compressed-column form -- col_ptr[n+1], and row_ids[nnz]
+ * holding for each column j the nodes i whose rows list j, ascending, once per listing.  Host
+ * buffers of n + 1 and nnz (efg_graph_csr) entries. */
+int efg_graph_csc(const efg_index* idx, uint64_t* col_ptr, uint32_t* row_ids);
+/* The same transpose of any CSR graph over n nodes held in host memory (no GPU involved):
+ * EFG_ERR_ARG when an id is >= n or row_ptr is not ascending. */
+int efg_csr_transpose(uint64_t n, const uint64_t* row_ptr, const uint32_t* ids, uint64_t* col_ptr,
+                      uint32_t* row_ids);
 /* Trees held by the index (0 if none). */
 uint32_t efg_tree_count(const efg_index* idx);
 

@@ -116,3 +116,17 @@ def test_device_resident_index_and_stats(efg):
     assert np.array_equal(a.graph(), b.graph())
     s = a.build_stats()
     assert s.join_pairs > 0 and s.merge_distances > 0 and s.total_ms > 0 and s.trees_ms > 0
+
+
+def test_graph_csc_is_the_transpose_of_the_graph(efg):
+    """getGraphMat (matlab/findex.cc:106-150): column j lists, ascending, the nodes whose rows hold j."""
+    x = datasets.mixture_u8(3000, 32, seed=4)
+    idx = efg.Index(x, efg.IndexParams(trees=4, merge_level=4, epochs=4))
+    idx.build_index()
+    g = idx.graph()
+    col_ptr, row_ids = idx.graph_csc()
+    assert col_ptr[-1] == g.size
+    src = np.repeat(np.arange(g.shape[0], dtype=np.uint32), g.shape[1])
+    order = np.lexsort((src, g.ravel()))  # by column, then by row
+    assert np.array_equal(row_ids, src[order])
+    assert np.array_equal(col_ptr[1:], np.cumsum(np.bincount(g.ravel(), minlength=g.shape[0])))

@@ -426,21 +426,19 @@ __global__ void bound_kernel(uint64_t n, uint32_t P, const float* __restrict__ p
 // of magnitude, so a fixed assignment leaves most warps of a block idle behind its longest node).
 // New entries are taken two at a time: x0 = new[p] pairs with Y = new[p+1..] + old, x1 = new[p+1]
 // with Y[1..], so every candidate row loaded serves both; four rows per pass, the 2 x 4 sums
-// reduced together.  With a node list (list[0] nodes, their ids from list[1]) only those nodes.
+// reduced together.
 __global__ void __launch_bounds__(256, 4) join_dist_kernel(
     const float* __restrict__ base, uint32_t ld4, uint64_t n, uint32_t cap, uint32_t P, uint32_t check_k,
     const uint32_t* __restrict__ new_ids, const uint32_t* __restrict__ new_cnt, const uint32_t* __restrict__ old_ids,
     const uint32_t* __restrict__ old_cnt, const uint64_t* __restrict__ pair_off, const float* __restrict__ bound,
     float* __restrict__ pairdist, uint32_t* __restrict__ cnt, uint8_t* __restrict__ found,
-    uint32_t* __restrict__ next_node, const uint32_t* __restrict__ list) {
+    uint32_t* __restrict__ next_node) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint64_t nodes = list ? list[0] : n;
   for (;;) {
     uint32_t ii = 0;
     if (lane == 0) ii = atomicAdd(next_node, 1u);
-    ii = __shfl_sync(0xffffffffu, ii, 0);
-    if (ii >= nodes) return;
-    const uint64_t i = list ? list[1 + ii] : ii;
+    const uint64_t i = __shfl_sync(0xffffffffu, ii, 0);
+    if (i >= n) return;
     const uint32_t nn = new_cnt[i], no = old_cnt[i];
     if (nn == 0) continue;
     const uint32_t* nw = new_ids + i * cap;
@@ -1163,7 +1161,7 @@ static int nnd_iterate_device(efg_index* idx, NNDev& S, uint32_t iter, uint64_t*
   } else {
     join_dist_kernel<<<jgrid0, 256, 0, s>>>(idx->d_base, ld4, n, S.cap, S.P, bp.check_k, S.new_ids.p, S.new_cnt.p,
                                             S.old_ids.p, S.old_cnt.p, S.pair_off.p, bound.p, S.pairdist.p, S.cnt.p,
-                                            S.found.p, jctr.p, nullptr);
+                                            S.found.p, jctr.p);
     EFG_CUDA(cudaGetLastError());
   }
   widen_kernel<<<blocks_for(n, 256), 256, 0, s>>>(S.cnt.p, tmp64.p, n);

@@ -68,6 +68,24 @@ def recall(res: np.ndarray, gt: np.ndarray, k: int = 10) -> float:
     return hits / (k * len(res))
 
 
+def recall_ties(res: np.ndarray, gt: np.ndarray, base: np.ndarray, queries: np.ndarray, k: int = 10,
+                chunk: int = 2048) -> float:
+    """Recall with exact ties counted: a returned id is a hit when its FP64 squared distance to the query
+    is at most that of the exact k-th neighbour (integer-valued data tie often, and the exact k-NN
+    then names one of several equally near points).  Ids outside the base (-1) are misses."""
+    n = base.shape[0]
+    hits = 0
+    for a in range(0, len(res), chunk):
+        r = np.asarray(res[a:a + chunk, :k], np.int64)
+        g = np.asarray(gt[a:a + chunk, :k], np.int64)
+        qq = np.asarray(queries[a:a + chunk], np.float64)[:, None, :]
+        kth = ((np.asarray(base[g], np.float64) - qq) ** 2).sum(-1).max(1)
+        ok = (r >= 0) & (r < n)
+        dr = ((np.asarray(base[np.where(ok, r, 0)], np.float64) - qq) ** 2).sum(-1)
+        hits += int(((dr <= kth[:, None]) & ok).sum())
+    return hits / (k * len(res))
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -285,8 +303,13 @@ def run_gpu(args):
         for _ in range(args.steps):
             idx.knn_search(10, q)
         e2e_s = time.perf_counter() - t0
+        try:
+            rc_ties = recall_ties(res_host, gt, x, q)
+        except Exception as e:  # a reported extra: never the reason the line is missing
+            log("recall with ties:", e)
+            rc_ties = None
         return {"precision": precision, "trees": trees, "point": point, "ladder": ladder, "config_recall": res_cfg,
-                "recall": recall(res_host, gt), "ms": ms, "per_step_ms": ms / args.steps,
+                "recall": recall(res_host, gt), "recall_ties": rc_ties, "ms": ms, "per_step_ms": ms / args.steps,
                 "value": replicas.throughput(nq * args.steps, ms / 1e3, ws),
                 "e2e": replicas.throughput(nq * args.steps, replicas.max_over_ranks(e2e_s, dev), ws),
                 "evals_q": evals_q, "exp_q": exp_q, "bytes_q": bytes_q, "launches": int(st.kernel_launches),
@@ -323,7 +346,8 @@ def run_gpu(args):
 
     def point_of(r):
         pt = r["point"]
-        return {"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(r["recall"], 4)}
+        return {"epochs": pt[0], "pool": pt[1], "extend": pt[2], "recall@10": round(r["recall"], 4),
+                "recall@10_with_ties": None if r["recall_ties"] is None else round(r["recall_ties"], 4)}
 
     f32, b16 = runs["fp32"], runs["bf16"]
 

@@ -78,3 +78,24 @@ def test_reference_arm_fails_when_the_build_fails():
     r = _bench("--impl", "reference", "--n", "1000", "--nq", "100", "--steps", "3", "--warmup", "3")
     assert r.returncode != 0
     assert "graph build failed with status 3" in r.stderr
+
+
+def test_recall_with_ties_counts_equally_near_points():
+    """An id as near as the exact k-th neighbour counts as a hit; -1 and farther ids do not."""
+    import numpy as np
+    import bench
+    base = np.array([[0.], [1.], [-1.], [2.], [5.]], np.float32)  # 1 and 2 are tied for the query 0
+    q = np.array([[0.]], np.float32)
+    gt = np.array([[0, 1]])
+    assert bench.recall_ties(np.array([[0, 2]]), gt, base, q, k=2) == 1.0    # the tie counts
+    assert bench.recall(np.array([[0, 2]]), gt, k=2) == 0.5                 # the strict recall does not
+    assert bench.recall_ties(np.array([[0, 3]]), gt, base, q, k=2) == 0.5    # farther: a miss
+    assert bench.recall_ties(np.array([[0, -1]]), gt, base, q, k=2) == 0.5   # not found: a miss
+    rng = np.random.default_rng(0)
+    x = rng.integers(0, 4, (300, 3)).astype(np.float32)
+    qq = rng.integers(0, 4, (40, 3)).astype(np.float32)
+    d = ((qq[:, None, :].astype(np.float64) - x[None]) ** 2).sum(-1)
+    exact = np.argsort(d, axis=1, kind="stable")[:, :10]
+    assert bench.recall_ties(exact, exact, x, qq) == 1.0
+    shuffled = np.argsort(d + rng.random(d.shape) * 1e-3, axis=1)[:, :10]  # other members of the ties
+    assert bench.recall_ties(shuffled, exact, x, qq) == 1.0

@@ -123,9 +123,12 @@ int efg_set_search_precision(efg_index* idx, int precision);
  * BF16 holds every value one product per value, else three (hi + lo split, a relative error near
  * 2^-17 of sum |x_k y_k|).  For integer data with squared norms below 2^23 (bytes up to 128
  * dimensions) every distance, and so the graph, equals the FP32 build's; for other data pools can
- * differ where distances tie within that error.  Several nodes share one tile of 128 new x 256
- * rows; a node with more is scored as blocks of its new entries x chunks of its candidates
- * (efg_build_stats.join_large_nodes counts them). */
+ * differ where distances tie within that error.  Several nodes share a tile of up to 128 new
+ * entries x 128 (or, for larger nodes, 256) rows; a node with more than 128 new entries or 256
+ * rows is scored as blocks of its new entries x chunks of its candidates
+ * (efg_build_stats.join_large_nodes counts them).  A pair already in a pool is rejected as a
+ * duplicate whatever its distance in this form (the reference compares ids among entries of equal
+ * distance), so an id that comes back a few ulps apart is not inserted twice. */
 int efg_set_build_precision(efg_index* idx, int precision);
 /* Bound on the nnexp search's per-query candidate buffer (no reference counterpart; the reference's
  * candidate vector grows without bound).  0, the default, sizes it for the worst case of one

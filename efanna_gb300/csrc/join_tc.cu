@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(JTHREADS, Tile<TR>::CTAS) tc_join_kernel(const
   __shared__ uint32_t rows_sh[TR];                 // the tile's rows: all new entries, then all old ones
   __shared__ float norm_sh[TR];
   __shared__ uint32_t tmem_base_sh, chn_sh, chpos_sh, tn_sh, nsum_sh, tsum_sh;
+  __shared__ uint32_t next_k0_sh, next_cn_sh;  // the chunk being fetched (published after a barrier)
   __shared__ int abort_sh, rec_fail_sh, bad_sh;
   // MODE_BIG: the node (id, list lengths, pair offset), the next tile's block of new entries and
   // candidate chunk start, whether it is the block's first (the one with the triangle), the tile
@@ -219,18 +220,22 @@ __global__ void __launch_bounds__(JTHREADS, Tile<TR>::CTAS) tc_join_kernel(const
       }
     } else {
       // ---------------------------------------------------------- packed tiles
-      if (chpos_sh >= chn_sh) {  // the chunk is packed: the next JCH nodes
+      // every thread reads the chunk position before thread 0 changes it (below, or in the packing
+      // step): a warp that read it late would take another branch and miss the barriers
+      const bool fetch = chpos_sh >= chn_sh;
+      __syncthreads();
+      if (fetch) {  // the chunk is packed: the next JCH nodes
         if (threadIdx.x == 0) {
           const uint32_t total = a.mode == MODE_LIST ? a.mid[0] : (uint32_t)a.n;
           const uint32_t k0 = *abort_flag ? total : atomicAdd(a.next_node, JCH);
-          chn_sh = k0 < total ? min(JCH, total - k0) : 0;
-          chpos_sh = k0;  // (the chunk's first position, for the loads below)
+          next_cn_sh = k0 < total ? min(JCH, total - k0) : 0;
+          next_k0_sh = k0;
         }
         __syncthreads();
-        const uint32_t cn = chn_sh;
+        const uint32_t cn = next_cn_sh;
         if (cn == 0) break;
         if (threadIdx.x < cn) {
-          const uint32_t k = chpos_sh + threadIdx.x;
+          const uint32_t k = next_k0_sh + threadIdx.x;
           const uint32_t i = a.mode == MODE_LIST ? a.mid[1 + k] : k;
           uint32_t nn = a.new_cnt[i];
           const uint32_t no = a.old_cnt[i];
@@ -248,7 +253,10 @@ __global__ void __launch_bounds__(JTHREADS, Tile<TR>::CTAS) tc_join_kernel(const
           po_ch[threadIdx.x] = a.pair_off[i];
         }
         __syncthreads();
-        if (threadIdx.x == 0) chpos_sh = 0;
+        if (threadIdx.x == 0) {
+          chn_sh = cn;
+          chpos_sh = 0;
+        }
       }
       if (threadIdx.x == 0) {  // the next nodes of the chunk that fit one tile together
         const uint32_t cn = chn_sh;

@@ -88,8 +88,7 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
 
 template <uint32_t TR>
 struct Tile {
-  // CTAs per SM: three 128-column accumulators (a quarter of TMEM left free: four CTAs of 128 rows,
-  // all 512 columns, stalled large builds), two of 256
+  // CTAs per SM: three 128-column accumulators, or two of 256 (of the SM's 512 TMEM columns)
   static constexpr uint32_t CTAS = TR == 128 ? 3 : 2;
   static constexpr uint32_t PART = TR * 128;  // one k-block of TR rows
   static constexpr uint32_t DLD = TR + 1;     // row stride of the Gram rows in shared memory
